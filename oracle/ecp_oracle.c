@@ -1,0 +1,1553 @@
+/*
+ * ecp_oracle.c -- TEST INFRASTRUCTURE ONLY (parity checker and CPU baseline).
+ *
+ * CPU restatement, in plain C and FP64, of chrr/libECP's ECP-integral path.
+ * It is pinned against the reference itself: the committed fixtures under
+ * tests/golden/ were produced by the unmodified reference (oracle/_ref, built
+ * by oracle/Makefile) and tests/test_oracle_golden.py requires this file to
+ * reproduce them.
+ *
+ * Structure (each part cites the reference code it restates):
+ *   tables     factorials, Cartesian ordering, cart->sph and poly->sph
+ *              matrices, Gauss-Chebyshev grids and their level schedules,
+ *              Bessel table, angular table Omega              (set-up)
+ *   centre     potential tabulation + screening, basis-set screening
+ *              windows, F tables                              (per ECP centre)
+ *   atom       real spherical harmonics at r_AC, angular contraction,
+ *              unit-sphere polynomials                        (per centre, atom)
+ *   block      type-1 (calcChi/calcQ), type-2 (calcGamma/calcT_*),
+ *              binomial shift (calcPolynomials)               (per pair, centre)
+ *
+ * The arithmetic of every formula is kept in the reference's operation order
+ * so that, compiled without FMA contraction, results agree with the
+ * reference to the last bit or nearly so; where the reference reads past the
+ * end of an array (basis l >= ECP L, tiny angular momenta) this file sizes its
+ * tables so the read is in bounds and computes what a padded reference
+ * computes (a zero-coefficient high-l ECP pad, which leaves every in-bounds
+ * value unchanged).  The reference's reuse of stale buffers inside its
+ * large-grid fallbacks is reproduced exactly, because those values do enter
+ * its results.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "ecp_oracle.h"
+
+#define NCART(l) (((l) + 1) * ((l) + 2) / 2)          /* IJK_DIM  */
+#define NCUM(l) (((l) + 1) * ((l) + 2) * ((l) + 3) / 6) /* C_DIM    */
+#define NSPH(l) (((l) + 1) * ((l) + 1))               /* L_DIM    */
+#define LM(l, m) ((l) * (l) + (m))                    /* m = 0..2l */
+
+static const double kPi = 3.14159265358979323846;
+
+/* ------------------------------------------------------------------ tables */
+
+/* n! (step 1) or n!! (step 2) for 0..n; src/util.c:57-100.  The reference
+ * leaves f[1] unset when n == 1 and reads past the end for small tmDim; the
+ * table here always has room for index `need` and f[0] = f[1] = 1. */
+static double *fact_table(int n, int step, int need) {
+  int top = n > need ? n : need;
+  double *f = calloc(top + 1, sizeof(double));
+  f[0] = 1.0;
+  if (top >= 1) f[1] = 1.0;
+  for (int i = 2; i <= top; i++) {
+    f[i] = f[i - step] * i;
+    if (isinf(f[i])) { free(f); return NULL; }
+  }
+  return f;
+}
+
+static double binom(int n, int k, const double *fac) {
+  /* src/util.c:105-113 */
+  return (k >= 0 && k <= n) ? fac[n] / (fac[n - k] * fac[k]) : 0.0;
+}
+
+/* Cartesian exponents in libint order (x^a y^b z^c, a descending, then b
+ * descending), three ints per function; src/dimensions.c:18-40. */
+static int *cart_order(int am) {
+  int *t = calloc(3 * NCUM(am), sizeof(int));
+  for (int l = 0; l <= am; l++) {
+    int c = 0;
+    for (int i = 0; i <= l; i++)
+      for (int j = 0; j <= i; j++, c++) {
+        int *e = t + 3 * (NCUM(l - 1) + c);
+        e[0] = l - i; e[1] = i - j; e[2] = j;
+      }
+  }
+  return t;
+}
+
+/* (a,b,c) -> running Cartesian index; src/dimensions.c:42-58. */
+static int *cart_index(int am, const int *ijk) {
+  int d = am + 1;
+  int *ix = calloc(d * d * d, sizeof(int));
+  for (int k = 0; k < NCUM(am); k++) {
+    const int *e = ijk + 3 * k;
+    ix[(e[0] * d + e[1]) * d + e[2]] = k;
+  }
+  return ix;
+}
+
+static int tm_dim(int l, const double *fac) { /* src/transformations.h:13 */
+  return (int)((3 * l + 2) * fac[l + 3] / (12 * fac[l]));
+}
+static int tm_index(int l, int m, int c, const double *fac) { /* transformations.h:14 */
+  return l == 0 ? 0 : tm_dim(l - 1, fac) + m * NCART(l) + c;
+}
+
+/* Cartesian -> real spherical transformation (Schlegel & Frisch eq. 15),
+ * blocks [l][m][c]; src/transformations.c:29-87. */
+static double *cart2sph_table(int lmax, const int *xyz, const double *fac) {
+  double *TM = calloc(tm_dim(lmax, fac), sizeof(double));
+  double *T = TM;
+  for (int l = 0; l <= lmax; l++)
+    for (int m = -l; m <= l; m++) {
+      int mm = abs(m);
+      for (int c = 0; c < NCART(l); c++, T++) {
+        const int *e = xyz + 3 * (NCUM(l - 1) + c);
+        int lx = e[0], ly = e[1], lz = e[2];
+        int j = lx + ly - mm;
+        if (j < 0 || j % 2 == 1) { *T = 0.0; continue; }
+        j /= 2;
+        double s1 = 0.0;
+        for (int i = 0; i <= (l - mm) / 2; i++) {
+          double s2 = 0.0;
+          for (int k = 0; k <= j; k++) {
+            double s = 0.0;
+            if ((m < 0 && abs(mm - lx) % 2 == 1) || (m > 0 && abs(mm - lx) % 2 == 0))
+              s = pow(-1.0, (mm - lx + 2 * k) / 2) * sqrt(2.0);
+            else if (m == 0 && lx % 2 == 0)
+              s = pow(-1.0, -lx / 2 + k);
+            s2 += binom(j, k, fac) * binom(mm, lx - 2 * k, fac) * s;
+          }
+          s1 += binom(l, i, fac) * binom(i, j, fac) * pow(-1.0, i) * fac[2 * l - 2 * i] /
+                fac[l - mm - 2 * i] * s2;
+        }
+        *T = sqrt((fac[2 * lx] * fac[2 * ly] * fac[2 * lz] * fac[l] * fac[l - mm]) /
+                  (fac[2 * l] * fac[lx] * fac[ly] * fac[lz] * fac[l + mm])) *
+             1 / (pow(2.0, l) * fac[l]) * s1;
+      }
+    }
+  return TM;
+}
+
+/* Expansion of unit-sphere polynomials in real spherical harmonics
+ * (Flores-Moreno et al. 2006, eq. 36): rows = running Cartesian index,
+ * columns = LM(l2, m); src/transformations.c:147-207. */
+static double *poly2sph_table(const double *M, int lmax, const int *xyz, const double *dfac) {
+  int ldim = NSPH(lmax);
+  double *TM = calloc((size_t)NCUM(lmax) * ldim, sizeof(double));
+  for (int l1 = 0; l1 <= lmax; l1++)
+    for (int c1 = 0; c1 < NCART(l1); c1++) {
+      const int *e1 = xyz + 3 * (NCUM(l1 - 1) + c1);
+      double *T = TM + (size_t)(NCUM(l1 - 1) + c1) * ldim;
+      const double *tcs = M;
+      for (int l2 = 0; l2 <= l1; l2++) {
+        double s1 = 4.0 * kPi * dfac[2 * l2 + 1];
+        for (int m = 0; m < 2 * l2 + 1; m++) {
+          double sum = 0.0;
+          for (int c2 = 0; c2 < NCART(l2); c2++, tcs++) {
+            const int *e2 = xyz + 3 * (NCUM(l2 - 1) + c2);
+            int lx = e1[0] + e2[0], ly = e1[1] + e2[1], lz = e1[2] + e2[2];
+            if (lx % 2 || ly % 2 || lz % 2) continue;
+            double s = s1, s2 = 1.0 / dfac[l1 + l2 + 1];
+            if (lx > 2) s2 *= dfac[lx - 1];
+            if (ly > 2) s2 *= dfac[ly - 1];
+            if (lz > 2) s2 *= dfac[lz - 1];
+            if (e2[0] > 1) s /= dfac[2 * e2[0] - 1];
+            if (e2[1] > 1) s /= dfac[2 * e2[1] - 1];
+            if (e2[2] > 1) s /= dfac[2 * e2[2] - 1];
+            sum += sqrt(s) * s2 * (*tcs);
+          }
+          *T++ = sum;
+        }
+      }
+    }
+  return TM;
+}
+
+/* --------------------------------------------------- Gauss-Chebyshev grids */
+
+/* A quadrature schedule lists, level by level, the lower-half abscissa
+ * indices the nested Gauss-Chebyshev rule adds (the upper-half partner of
+ * index i is order-1-i), so the adaptive integrators below are a walk over a
+ * fixed table.  Built by simulating the index arithmetic of
+ * src/gc_integrators.c:157-217 (PS93) and :39-86 (PSM92). */
+typedef struct {
+  int order;
+  int head[3];        /* PS93: mid, q-lower, q-upper.  PSM92: mid only. */
+  int nLevels;
+  int lvStart[32];    /* offsets into idx[] */
+  int lvCount[32];
+  int lvJ[32];        /* PS93 switch j for the level (1 two-point, 0 one-point) */
+  int lvN[32];        /* n after the level */
+  int *idx;
+} Sched;
+
+typedef struct {
+  int order;
+  double *x, *w;
+  double tol;
+  Sched sch;
+} Grid;
+
+static void sched_ps93(Sched *s, int nParam) {
+  int runs = (int)floor(log(nParam) / log(2));
+  int offset = (int)pow(2, runs);
+  int order = 3 * offset - 1;
+  int n = 3, j = 0, k = 0, total = 0;
+  s->order = order;
+  s->head[0] = (order - 1) / 2;
+  s->head[1] = offset - 1;
+  s->head[2] = order - offset;
+  s->idx = calloc(order, sizeof(int));
+  offset /= 2;
+  while ((2 * n * (1 - j) + j * 4 * n / 3 - 1) <= order) {
+    j = 1 - j;
+    if (j == 0) offset /= 2;
+    s->lvStart[k] = total;
+    for (int i = 1; i < n; i += 2)
+      if (3 * ((i + 2 * j) / 3) >= i + j) s->idx[total++] = i * offset - 1;
+    s->lvCount[k] = total - s->lvStart[k];
+    n *= (1 + j);
+    s->lvJ[k] = j;
+    s->lvN[k] = n;
+    k++;
+  }
+  s->nLevels = k;
+}
+
+static void sched_psm92(Sched *s, int order) {
+  int ord = (int)pow(2, floor(log(order + 1) / log(2))) - 1;
+  int runs = (int)floor(log(ord) / log(2));
+  int offset = (int)pow(2, runs);
+  int M = (ord - 1) / 2, n = 1, k = 0, total = 0;
+  s->order = ord;
+  s->head[0] = M;
+  s->idx = calloc(ord, sizeof(int));
+  while (n <= M) {
+    offset /= 2;
+    s->lvStart[k] = total;
+    for (int i = 1; i <= n; i += 2) s->idx[total++] = i * offset - 1;
+    s->lvCount[k] = total - s->lvStart[k];
+    n = 2 * n + 1;
+    s->lvJ[k] = 0;
+    s->lvN[k] = n;
+    k++;
+  }
+  s->nLevels = k;
+}
+
+/* PS93 abscissae/weights on (-1,1), then the Krack-Koster map to (0,inf);
+ * src/gc_integrators.c:221-283 and :302-315. */
+static void grid_ps93(Grid *g, int maxPoints, double tol) {
+  int runs = (int)floor(log(maxPoints) / log(2));
+  int offset = (int)pow(2, runs);
+  int order = 3 * offset - 1, n = 3;
+  double C0 = sin(kPi / 3), S0 = 0.5, C1 = S0, S1 = C0, c, s, s2, t;
+  g->order = order;
+  g->tol = tol;
+  g->x = calloc(order, sizeof(double));
+  g->w = calloc(order, sizeof(double));
+  double *x = g->x, *w = g->w;
+  c = cos(kPi / 3);
+  s = C0;
+  s2 = s * s;
+  x[order / 2] = 0.0;
+  w[order / 2] = 1.0;
+  t = (n - 2.0) / n + 2 / kPi * (1 + 2 * s2 / 3) * c * s;
+  x[offset - 1] = -t;
+  x[order - offset] = t;
+  w[order - offset] = w[offset - 1] = s2 * s2;
+  while ((4 * n / 3 - 1) <= order) {
+    c = C0;
+    s = S0;
+    offset /= 2;
+    for (int i = 1; i < n; i += 2) {
+      int idx = i * offset - 1;
+      s2 = s * s;
+      t = 1 + 2 / (3 * kPi) * s * c * (3 + 2 * s2) - ((double)i) / n;
+      x[idx] = -t;
+      x[order - idx - 1] = t;
+      w[order - idx - 1] = w[idx] = s2 * s2;
+      t = s;
+      s = s * C1 + c * S1;
+      c = c * C1 - t * S1;
+    }
+    n *= 2;
+    C1 = C0;
+    S1 = S0;
+    C0 = sqrt((1 + C0) / 2);
+    S0 = S0 / (2 * C0);
+  }
+  double ln2 = log(2.0);
+  for (int i = 0; i < order; i++) {
+    double xi = 1.0 - log(1.0 - x[i]) / ln2;
+    double wi = w[i] / (ln2 * (1.0 - x[i]));
+    x[i] = xi;
+    w[i] = wi;
+  }
+  sched_ps93(&g->sch, maxPoints);
+}
+
+/* PSM92 abscissae/weights on (-1,1); src/gc_integrators.c:90-145. */
+static void grid_psm92(Grid *g, int maxPoints, double tol) {
+  int order = (int)pow(2, floor(log(maxPoints + 1) / log(2))) - 1;
+  int runs = (int)floor(log(order) / log(2));
+  int offset = (int)pow(2, runs);
+  int M = (order - 1) / 2, n = 1;
+  double N = n + 1.0, S0 = 1.0, C0 = 0.0, S1, C1, s, c, t;
+  g->order = order;
+  g->tol = tol;
+  g->x = calloc(order, sizeof(double));
+  g->w = calloc(order, sizeof(double));
+  double *x = g->x, *w = g->w;
+  x[M] = 0.0;
+  w[M] = 1.0;
+  while (n <= M) {
+    C1 = C0;
+    S1 = S0;
+    C0 = sqrt((1 + C1) / 2);
+    S0 = S1 / (2 * C0);
+    s = S0;
+    c = C0;
+    offset /= 2;
+    for (int i = 1; i <= n; i += 2) {
+      t = 1 + 2 / (3 * kPi) * (3 + 2 * s * s) * s * c - i / N;
+      int idx = i * offset - 1;
+      x[order - idx - 1] = t;
+      x[idx] = -t;
+      w[order - idx - 1] = w[idx] = s * s * s * s;
+      t = s;
+      s = s * C1 + c * S1;
+      c = c * C1 - t * S1;
+    }
+    n = 2 * n + 1;
+    N = n + 1.0;
+  }
+  sched_psm92(&g->sch, order);
+}
+
+/* Linear Flores-Moreno map of (-1,1) to [max(0,P-7s), P+9s], s = 1/sqrt(zeta_P);
+ * src/gc_integrators.c:317-331.  Writes into x/w (copies of the raw grid). */
+static void map_fm06(int n, const double *x0, const double *w0, double *x, double *w,
+                     double zetaP, double P) {
+  double sigma = 1.0 / sqrt(zetaP);
+  double t = P - 7.0 * sigma;
+  double rmin = (t > 0.0) ? t : 0.0;
+  double rmax = P + 9.0 * sigma;
+  double i1 = 0.5 * (rmax - rmin);
+  double i2 = 0.5 * (rmax + rmin);
+  for (int i = 0; i < n; i++) {
+    x[i] = i1 * x0[i] + i2;
+    w[i] = w0[i] * i1;
+  }
+}
+
+typedef double (*Integrand)(int idx, const void *ctx);
+
+/* Adaptive PS93 walk (src/gc_integrators.c:157-217): absolute error test,
+ * lower-half points counted only at or after `start`, upper-half points only
+ * at or before `end`, levels that touch no point skip the test. */
+static int quad_ps93(const Sched *s, const double *w, int start, int end, double tol,
+                     Integrand f, const void *ctx, double *res, OracleStats *st) {
+  int order = s->order, n = 3;
+  double p = w[s->head[0]] * f(s->head[0], ctx);
+  double q = w[s->head[1]] * f(s->head[1], ctx) + w[s->head[2]] * f(s->head[2], ctx);
+  double I = p + q, err = 0.0;
+  long long pts = 3;
+  st->ps93_calls++;
+  for (int k = 0; k < s->nLevels; k++) {
+    int j = s->lvJ[k], cnt = 0;
+    const int *lv = s->idx + s->lvStart[k];
+    for (int t = 0; t < s->lvCount[k]; t++) {
+      int lo = lv[t], hi = order - lo - 1;
+      double T = 0.0;
+      if (lo >= start) { T += w[lo] * f(lo, ctx); cnt++; }
+      if (hi <= end) { T += w[hi] * f(hi, ctx); cnt++; }
+      I += T;
+    }
+    pts += cnt;
+    n = s->lvN[k];
+    p += (1 - j) * (I - q);
+    if (cnt > 0) err = 16 * fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q)) / (3 * n);
+    q = (1 - j) * q + j * I;
+    if (cnt == 0) continue;
+    if (err < tol) {
+      *res = 16 * q / (3 * n);
+      st->ps93_points += pts;
+      return 0;
+    }
+  }
+  st->ps93_points += pts;
+  st->ps93_failed++;
+  return 1;
+}
+
+/* Adaptive PSM92 walk (src/gc_integrators.c:39-86): relative-type test
+ * 16 e^2 <= 3 N |I - q| tol. */
+static int quad_psm92(const Sched *s, const double *w, int start, int end, double tol,
+                      Integrand f, const void *ctx, double *res, OracleStats *st) {
+  int order = s->order, M = s->head[0];
+  double I = w[M] * f(M, ctx), p = I, q, e, N;
+  long long pts = 1;
+  st->psm92_calls++;
+  for (int k = 0; k < s->nLevels; k++) {
+    int cnt = 0;
+    const int *lv = s->idx + s->lvStart[k];
+    q = 2 * p;
+    p = 2 * I;
+    for (int t = 0; t < s->lvCount[k]; t++) {
+      int lo = lv[t], hi = order - lo - 1;
+      double T = 0.0;
+      if (lo >= start) { T += w[lo] * f(lo, ctx); cnt++; }
+      if (hi <= end) { T += w[hi] * f(hi, ctx); cnt++; }
+      I += T;
+    }
+    pts += cnt;
+    N = s->lvN[k] + 1.0;
+    e = I - p;
+    if (cnt == 0) continue;
+    if (16 * e * e <= 3 * N * fabs(I - q) * tol) {
+      *res = 16 * I / (3 * N);
+      st->psm92_points += pts;
+      return 0;
+    }
+  }
+  st->psm92_points += pts;
+  st->psm92_failed++;
+  return 1;
+}
+
+/* ------------------------------------------------------------------ Bessel */
+
+typedef struct {
+  int lMax, N, dim;
+  double *K; /* [lMax+1][N+1] */
+  double *C; /* [lMax+1], C[i] = i/(2i+1) */
+} Bessel;
+
+/* Series table of K_l(z) = exp(-z) i_l(z) at z = i/(N/16); src/bessel.c:20-82. */
+static int bessel_table(Bessel *b, int lMax, int N, int cutoff, double accuracy) {
+  double *F = malloc((cutoff + 1) * sizeof(double));
+  double *G = malloc((cutoff + lMax + 2) * sizeof(double));
+  int dim = N + 1;
+  b->lMax = lMax; b->N = N; b->dim = dim;
+  b->K = calloc((size_t)(lMax + 1) * dim, sizeof(double));
+  b->C = calloc(lMax + 1, sizeof(double));
+  b->K[0] = 1.0;
+  for (int i = 1; i <= N; i++) {
+    double z = i / (N / 16.0), f = z * z / 2.0, s;
+    int j = 0, l;
+    F[0] = exp(-z);
+    G[0] = 1.0;
+    s = F[0] / G[0];
+    l = (int)(0.25 * sqrt(1.0 + 16.0 * f));
+    while (s > accuracy || j <= l) {
+      b->K[i] += s;
+      j++;
+      if (j > cutoff) { free(F); free(G); return 1; }
+      F[j] = F[j - 1] * f / j;
+      G[j] = G[j - 1] * (2.0 * j + 1.0);
+      s = F[j] / G[j];
+    }
+    for (l = 1; l <= lMax; l++) G[j + l] = G[j + l - 1] * (2 * j + 2 * l + 1);
+    f = z;
+    for (l = 1; l <= lMax; l++) {
+      s = 0;
+      for (int m = 0; m < j; m++) s += F[m] / G[l + m];
+      b->K[(size_t)l * dim + i] = f * s;
+      f *= z;
+    }
+  }
+  for (int i = 1; i <= lMax; i++) b->C[i] = i / (2.0 * i + 1.0);
+  free(F);
+  free(G);
+  return 0;
+}
+
+/* K_0..K_lmax at one argument, written with stride `stride`; three branches
+ * (small z, 5-term Taylor about the nearest table point, asymptotic);
+ * src/bessel.c:102-199. */
+static void bessel_eval(const Bessel *b, int lmax, double z, double *K, int stride, OracleStats *st) {
+  st->bessel_calls++;
+  st->bessel_rows += lmax + 1;
+  if (z < 1.0E-7) {
+    if (z <= 0) {
+      K[0] = 1.0;
+      for (int l = 1; l <= lmax; l++) K[l * stride] = 0.0;
+    } else {
+      K[0] = 1 - z;
+      for (int l = 1; l <= lmax; l++) K[l * stride] = K[(l - 1) * stride] * z / (2 * l + 1);
+    }
+  } else if (z < 16.0) {
+    int top = lmax + 5;
+    double d[64], prev[64];
+    double h = b->N / 16; /* integer division, as in the reference */
+    int index = (int)floor(z * h + 0.5);
+    double dz = z - index / h, scale = 1.0;
+    for (int l = 0; l <= top; l++) d[l] = b->K[(size_t)l * b->dim + index];
+    for (int l = 0; l <= lmax; l++) K[l * stride] = d[l];
+    for (int i = 1; i <= 5; i++) {
+      int ti = top - i;
+      for (int j = 0; j <= ti + 1; j++) prev[j] = d[j];
+      d[0] = prev[1] - prev[0];
+      for (int j = 1; j <= ti; j++)
+        d[j] = b->C[j] * (prev[j - 1] - prev[j + 1]) - prev[j] + prev[j + 1];
+      scale = scale * dz / i;
+      for (int j = 0; j <= lmax; j++) K[j * stride] += scale * d[j];
+    }
+  } else {
+    double A[64];
+    A[0] = 0.5 / z;
+    for (int l = 0; l <= lmax; l++) K[l * stride] = A[0];
+    for (int l = 1; l <= lmax; l++) {
+      double f = l * (l + 1);
+      for (int i = 1; i < l; i++) {
+        K[l * stride] += f * A[i];
+        f *= (l + i + 1) * (l - i);
+      }
+      A[l] = -A[0] * A[l - 1] / l;
+      K[l * stride] += f * A[l];
+    }
+  }
+}
+
+/* ------------------------------------------------ spherical harmonics etc. */
+
+/* (r, theta, phi) of a Cartesian vector; src/util.c:75-106. */
+static void to_spherical(const double *v, double *out) {
+  const double eps = 1.0E-14;
+  double x = v[0], y = v[1], z = v[2];
+  double r = sqrt(x * x + y * y + z * z), th, ph;
+  th = (r < eps) ? 0.0 : acos(z / r);
+  if (fabs(x) < eps) {
+    if (fabs(y) < eps) ph = 0.0;
+    else if (y < 0.0) ph = 1.5 * kPi;
+    else ph = 0.5 * kPi;
+  } else {
+    ph = (x > 0.0) ? atan(y / x) : atan(y / x) + kPi;
+  }
+  out[0] = r; out[1] = th; out[2] = ph;
+}
+
+/* Normalised real spherical harmonics S_lm, index LM(l, m + l);
+ * associated Legendre recursion; src/spherical_harmonics.c:16-114. */
+static void real_sph(int lmax, double theta, double phi, const double *fac, const double *dfac,
+                     double *rsh) {
+  int n = NSPH(lmax);
+  double P[128], s[24], c[24];
+#define PL(l, m) P[(l) * (l) + (m) + (l)]
+  memset(P, 0, n * sizeof(double));
+  memset(s, 0, sizeof s);
+  memset(c, 0, sizeof c);
+  double x = cos(theta);
+  if (1.0 == x) {
+    for (int l = 0; l <= lmax; l++) PL(l, 0) = 1.0;
+  } else if (-1.0 == x) {
+    PL(0, 0) = 1.0;
+    for (int l = 1; l <= lmax; l++) PL(l, 0) = -PL(l - 1, 0);
+  } else {
+    s[1] = sqrt(1.0 - x * x);
+    for (int l = 2; l <= lmax; l++) s[l] = s[l - 1] * s[1];
+    for (int l = 0; l <= lmax; l++) {
+      if (l == 0) { PL(0, 0) = 1.0; continue; }
+      PL(l, l) = s[l] * dfac[2 * l - 1];
+      int m = l - 1;
+      PL(l, m) = x * (2 * m + 1) * PL(l - 1, m);
+      if (l > 1)
+        for (m = 0; m <= l - 2; m++)
+          PL(l, m) = (x * (2 * l - 1) * PL(l - 1, m) - (l + m - 1) * PL(l - 2, m)) / (l - m);
+    }
+  }
+  for (int l = 0; l <= lmax; l++) {
+    double norm0 = sqrt((2.0 * l + 1.0) / (2.0 * kPi));
+    PL(l, 0) = norm0 * PL(l, 0);
+    for (int m = 1; m <= l; m++) {
+      double norm = sqrt(fac[l - m] / fac[l + m]) * norm0;
+      PL(l, m) = norm * PL(l, m);
+    }
+  }
+  if (lmax > 0) {
+    if (0.0 == phi) {
+      for (int m = 0; m <= lmax; m++) { s[m] = 0.0; c[m] = 1.0; }
+    } else {
+      s[1] = sin(phi);
+      c[1] = cos(phi);
+      for (int m = 2; m <= lmax; m++) {
+        s[m] = s[1] * c[m - 1] + c[1] * s[m - 1];
+        c[m] = c[1] * c[m - 1] - s[1] * s[m - 1];
+      }
+    }
+  }
+  for (int l = 0; l <= lmax; l++) {
+    rsh[l * l + l] = PL(l, 0) / sqrt(2.0);
+    for (int m = 1; m <= l; m++) {
+      rsh[l * l + l - m] = PL(l, m) * s[m];
+      rsh[l * l + l + m] = PL(l, m) * c[m];
+    }
+  }
+#undef PL
+}
+
+/* ------------------------------------------------------------- the system */
+
+typedef struct {
+  /* input (borrowed) */
+  int nAtoms;
+  const double *geom;
+  const int *lBS, *KBS;
+  const double *dBS, *aBS;
+  /* basis */
+  int nShells;
+  int *shAtom, *shPrim, *shAO, *atomShell0, *atomNShell, *atomMaxL;
+  int dim;
+  /* ECP per atom: L (-1 = none), term range */
+  int *ecpL, *ecpT0, *ecpNT;
+  int *termL;
+  const double *termN, *termD, *termA;
+  /* global maxima */
+  int maxLECP, maxLBS, maxAlpha, maxLambda, tmDim, nk, tabL;
+  double *fac, *dfac;
+  int *ijk, *ijkIdx, ijkDim;
+  double *c2s, *p2s;
+  Grid small, large;
+  Bessel bes;
+  double *omega;
+  int omD1, omD2; /* omega dims [NSPH(maxL)][omD1][omD2] */
+  double acc, lnAcc1, lnAcc2, tol;
+} Sys;
+
+static void sys_free(Sys *S) {
+  free(S->shAtom); free(S->shPrim); free(S->shAO); free(S->atomShell0);
+  free(S->atomNShell); free(S->atomMaxL); free(S->ecpL); free(S->ecpT0);
+  free(S->ecpNT); free(S->termL); free(S->fac); free(S->dfac); free(S->ijk);
+  free(S->ijkIdx); free(S->c2s); free(S->p2s); free(S->small.x); free(S->small.w);
+  free(S->small.sch.idx); free(S->large.x); free(S->large.w); free(S->large.sch.idx);
+  free(S->bes.K); free(S->bes.C); free(S->omega);
+  free((void *)S->termN);
+}
+
+/* Angular table Omega[lm][lambda mu][Cartesian alpha]; basis- and
+ * ECP-independent; src/angular_integrals.c:16-101. */
+static void omega_table(Sys *S) {
+  int maxL = S->maxLECP, tmW = NSPH(S->tmDim);
+  S->omD1 = NSPH(S->maxLambda);
+  S->omD2 = NCUM(S->maxAlpha);
+  int inc1 = S->omD2, inc2 = S->omD1 * S->omD2, d = S->ijkDim;
+  S->omega = calloc((size_t)NSPH(maxL) * inc2 + 1, sizeof(double));
+  for (int lam = 0; lam <= S->maxLambda; lam++)
+    for (int l = 0; l < maxL; l++) {
+      int par = (lam + l) % 2, lo = lam - l;
+      int minAlpha = par > lo ? par : lo;
+      for (int alpha = minAlpha; alpha <= S->maxAlpha; alpha += 2)
+        for (int mu = 0; mu < 2 * lam + 1; mu++)
+          for (int m = 0; m < 2 * l + 1; m++) {
+            double *cijk = S->omega + LM(l, m) * inc2 + LM(lam, mu) * inc1 + NCUM(alpha - 1);
+            for (int c = 0; c < NCART(alpha); c++) {
+              const int *e = S->ijk + 3 * (NCUM(alpha - 1) + c);
+              if (alpha == 0) {
+                if (l == lam && m == mu) cijk[c] = 1.0;
+              } else if (lam <= l + alpha) {
+                for (int dd = 0; dd < NCART(l); dd++) {
+                  const int *f = S->ijk + 3 * (NCUM(l - 1) + dd);
+                  double N = 0.25 * S->dfac[2 * l + 1] / kPi;
+                  if (f[0] > 1) N /= S->dfac[2 * f[0] - 1];
+                  if (f[1] > 1) N /= S->dfac[2 * f[1] - 1];
+                  if (f[2] > 1) N /= S->dfac[2 * f[2] - 1];
+                  N = sqrt(N);
+                  int p = S->ijkIdx[((f[0] + e[0]) * d + (f[1] + e[1])) * d + (f[2] + e[2])];
+                  cijk[c] += N * S->c2s[tm_index(l, m, dd, S->fac)] * S->p2s[(size_t)p * tmW + LM(lam, mu)];
+                }
+              }
+            }
+          }
+    }
+}
+
+static int sys_build(Sys *S, int nrAtoms, const double *geometry, const int *shellsECP,
+                     const int *KECP, const int *lECP, const double *nECP, const double *dECP,
+                     const double *aECP, const int *shellsBS, const int *lBS, const int *KBS,
+                     const double *dBS, const double *aBS, int largeGridOrder, double tolerance,
+                     double accuracy) {
+  memset(S, 0, sizeof *S);
+  if (nrAtoms < 1 || nrAtoms > (1 << 24)) return 3;
+  S->nAtoms = nrAtoms;
+  S->geom = geometry;
+  S->lBS = lBS; S->KBS = KBS; S->dBS = dBS; S->aBS = aBS;
+  S->acc = accuracy;
+  S->tol = tolerance;
+  S->lnAcc1 = log(accuracy) - 2;   /* type 1 uses the caller's accuracy, libecp.c:90 */
+  S->lnAcc2 = log(1.0E-14) - 2;    /* type 2 is fixed at 1e-14, type2.c:58-59     */
+
+  /* basis bookkeeping */
+  int ns = 0;
+  for (int i = 0; i < nrAtoms; i++) ns += shellsBS[i];
+  S->nShells = ns;
+  S->shAtom = calloc(ns + 1, sizeof(int));
+  S->shPrim = calloc(ns + 1, sizeof(int));
+  S->shAO = calloc(ns + 1, sizeof(int));
+  S->atomShell0 = calloc((size_t)nrAtoms + 1, sizeof(int));
+  S->atomNShell = calloc((size_t)nrAtoms + 1, sizeof(int));
+  S->atomMaxL = calloc((size_t)nrAtoms + 1, sizeof(int));
+  int s = 0, p = 0, ao = 0;
+  S->maxLBS = 0;
+  for (int i = 0; i < nrAtoms; i++) {
+    S->atomShell0[i] = s;
+    S->atomNShell[i] = shellsBS[i];
+    for (int j = 0; j < shellsBS[i]; j++, s++) {
+      S->shAtom[s] = i; S->shPrim[s] = p; S->shAO[s] = ao;
+      p += KBS[s];
+      ao += NCART(lBS[s]);
+      if (lBS[s] > S->atomMaxL[i]) S->atomMaxL[i] = lBS[s];
+      if (lBS[s] > S->maxLBS) S->maxLBS = lBS[s];
+    }
+  }
+  S->dim = ao;
+
+  /* ECPs: per atom the shells' terms, in order (libecp.c:93-127) */
+  S->ecpL = calloc((size_t)nrAtoms + 1, sizeof(int));
+  S->ecpT0 = calloc((size_t)nrAtoms + 1, sizeof(int));
+  S->ecpNT = calloc((size_t)nrAtoms + 1, sizeof(int));
+  int nsh = 0, nt = 0;
+  for (int i = 0; i < nrAtoms; i++) {
+    for (int j = 0; j < shellsECP[i]; j++) { nt += KECP[nsh + j]; }
+    nsh += shellsECP[i];
+  }
+  S->termL = calloc(nt + 1, sizeof(int));
+  S->termN = nECP; S->termD = dECP; S->termA = aECP;
+  /* nECP is copied so the struct owns one pointer it may free uniformly */
+  double *nc = malloc((nt + 1) * sizeof(double));
+  for (int t = 0; t < nt; t++) nc[t] = nECP[t];
+  S->termN = nc;
+  nsh = nt = 0;
+  S->maxLECP = 0;
+  for (int i = 0; i < nrAtoms; i++) {
+    S->ecpL[i] = -1;
+    S->ecpT0[i] = nt;
+    if (shellsECP[i] > 0) {
+      int L = 0;
+      for (int j = 0; j < shellsECP[i]; j++, nsh++) {
+        if (lECP[nsh] > L) L = lECP[nsh];
+        for (int k = 0; k < KECP[nsh]; k++) S->termL[nt++] = lECP[nsh];
+      }
+      S->ecpL[i] = L;
+      if (L > S->maxLECP) S->maxLECP = L;
+    }
+    S->ecpNT[i] = nt - S->ecpT0[i];
+  }
+
+  S->maxAlpha = S->maxLBS;
+  S->maxLambda = S->maxLECP - 1 + S->maxAlpha;
+  S->tmDim = S->maxLambda + S->maxAlpha;
+  if (S->tmDim < 2 * S->maxLBS) S->tmDim = 2 * S->maxLBS;
+  if (S->maxLambda < 0 || S->tmDim > 20) return 3;
+  S->nk = S->maxLambda > 2 * S->maxLBS ? S->maxLambda + 1 : 2 * S->maxLBS + 1;
+  int nfac = 2 * (S->maxLambda + S->maxAlpha) + 1;
+  S->fac = fact_table(nfac, 1, 2 * S->tmDim + 4);
+  S->dfac = fact_table(nfac, 2, 2 * S->tmDim + 4);
+  if (!S->fac || !S->dfac) return 1;
+  S->ijkDim = S->tmDim + 1;
+  S->ijk = cart_order(S->tmDim);
+  S->ijkIdx = cart_index(S->tmDim, S->ijk);
+  S->c2s = cart2sph_table(S->tmDim, S->ijk, S->fac);
+  S->p2s = poly2sph_table(S->c2s, S->tmDim, S->ijk, S->dfac);
+
+  grid_psm92(&S->large, largeGridOrder, tolerance);
+  grid_ps93(&S->small, 128, tolerance);
+
+  S->tabL = S->maxLECP + S->maxAlpha + 6;
+  if (S->tabL < 2 * S->maxLBS + 5) S->tabL = 2 * S->maxLBS + 5;
+  if (bessel_table(&S->bes, S->tabL, 16 * 100, 200, accuracy)) return 1;
+  omega_table(S);
+  return 0;
+}
+
+/* U_l(r) = sum over the centre's terms with that l of d r^n exp(-a r^2);
+ * src/ecp.c:42-60. */
+static double eval_ecp(const Sys *S, int C, int l, double r, OracleStats *st) {
+  double pot = 0.0, r2 = r * r;
+  for (int t = S->ecpT0[C]; t < S->ecpT0[C] + S->ecpNT[C]; t++)
+    if (S->termL[t] == l) {
+      st->exp_calls++;
+      pot += pow(r, S->termN[t]) * S->termD[t] * exp(-S->termA[t] * r2);
+    }
+  return pot;
+}
+
+static double dist(const double *a, const double *b) { /* src/util.c:110-117 */
+  double x = a[0] - b[0], y = a[1] - b[1], z = a[2] - b[2];
+  return sqrt(x * x + y * y + z * z);
+}
+
+/* Newton radius of c r^l exp(-zeta r^2) = cutoff, returned squared;
+ * src/util.c:134-172.  Returns -1 when Newton does not converge (the
+ * reference asserts). */
+static double gto_radius(double c, double zeta, int l, double cutoff) {
+  double delta, dg, guess, zr, r;
+  const double t = log(fabs(c) / fabs(cutoff));
+  dg = t / zeta;
+  r = (dg > cutoff) ? dg : cutoff;
+  if (l != 0) {
+    int ok = 0;
+    if (l > 0) {
+      dg = sqrt(0.5 * l / fabs(c));
+      guess = (dg > cutoff) ? dg : cutoff;
+      if (guess > r) r = 0.5 * (r + guess);
+    }
+    for (int i = 0; i < 40; i++) {
+      zr = zeta * r;
+      guess = t + l * log(r) - zr * r;
+      delta = guess / (l / r - 2 * zr);
+      dg = r - delta;
+      r = (dg > cutoff) ? dg : cutoff;
+      if (fabs(delta) < cutoff) { r *= r; ok = 1; break; }
+    }
+    if (!ok) return -1.0;
+  }
+  return r;
+}
+
+/* src/util.c:178-192: radius of the most diffuse primitive with d != 0. */
+static double shell_radius(const Sys *S, int sh) {
+  const double *d = S->dBS + S->shPrim[sh], *a = S->aBS + S->shPrim[sh];
+  double zeta = a[0], c = fabs(d[0]);
+  for (int i = 1; i < S->KBS[sh]; i++)
+    if (a[i] < zeta && d[i] != 0.0) { zeta = a[i]; c = fabs(d[i]); }
+  double r = gto_radius(c, zeta, S->lBS[sh], 1.0E-14);
+  return r < 0 ? -1.0 : sqrt(r);
+}
+
+/* ------------------------------------------------------- per-centre data */
+
+typedef struct {
+  int C, L, gridEnd;
+  double rC[3];
+  double *utab;   /* [L][nk][order] */
+  double *uL;     /* [order] */
+  int *ws, *we, *skip;
+  double *F;      /* [nShells][nk][order] */
+  double **omA, **uspA;
+  double (*rAC)[3];
+  double *dAC;
+  int uspDim;
+} Centre;
+
+static int potential_screen(int start, int end, const double *U, double zero) {
+  for (int i = end; i >= start; i--)
+    if (fabs(U[i]) > zero) return i; /* src/util.c:199-212 */
+  return -1;
+}
+
+/* Unit-sphere polynomial table (-x)^i (-y)^j (-z)^k, i+j+k <= l, dims
+ * (l+1)^3; src/util.c:215-243. */
+static double *usp_table(int l, const double *r) {
+  int d = l + 1;
+  double *t = calloc((size_t)d * d * d, sizeof(double));
+  double x = 1.0, y = 1.0, z = 1.0;
+  for (int i = 0; i <= l; i++) {
+    x = (i == 0) ? 1.0 : -x * r[0];
+    for (int j = 0; j <= l - i; j++) {
+      y = (j == 0) ? 1.0 : -y * r[1];
+      for (int k = 0; k <= l - i - j; k++) {
+        z = (k == 0) ? 1.0 : -z * r[2];
+        t[(i * d + j) * d + k] = x * y * z;
+      }
+    }
+  }
+  return t;
+}
+
+/* A[lambda][lm][Cartesian] = sum_mu S_lambda,mu(r_A) Omega[lm][lambda mu][.];
+ * src/angular_integrals.c:105-142. */
+static double *angular_table(const Sys *S, int lmaxA, const double *rA) {
+  int maxL = S->maxLECP, lmax = maxL - 1 + lmaxA;
+  int inc1 = S->omD2, inc2 = S->omD1 * S->omD2;
+  int aInc1 = NCUM(lmaxA), aInc2 = S->omD1 * aInc1;
+  double R[3], rsh[400];
+  double *A = calloc((size_t)(lmax + 1) * aInc2 + 1, sizeof(double));
+  to_spherical(rA, R);
+  real_sph(lmax, R[1], R[2], S->fac, S->dfac, rsh);
+  for (int l = 0; l < maxL; l++)
+    for (int m = 0; m < 2 * l + 1; m++)
+      for (int lam = 0; lam <= lmax; lam++)
+        for (int la = 0; la <= lmaxA; la++)
+          for (int c = 0; c < NCART(la); c++) {
+            double v = 0.0;
+            for (int mu = 0; mu < 2 * lam + 1; mu++)
+              v += rsh[LM(lam, mu)] * S->omega[LM(l, m) * inc2 + LM(lam, mu) * inc1 + NCUM(la - 1) + c];
+            A[lam * aInc2 + LM(l, m) * aInc1 + NCUM(la - 1) + c] = v;
+          }
+  return A;
+}
+
+static void centre_free(Centre *c, int nAtoms) {
+  free(c->utab); free(c->uL); free(c->ws); free(c->we); free(c->skip); free(c->F);
+  if (c->omA)
+    for (int i = 0; i < nAtoms; i++) { free(c->omA[i]); free(c->uspA[i]); }
+  free(c->omA); free(c->uspA); free(c->rAC); free(c->dAC);
+}
+
+/* Per-centre tables: tabECP_FM06 (type2.c:185-219), U_L (libecp.c:268-271),
+ * calcF_FM06 with basis-set screening (type2.c:223-310, :149-180), and per
+ * atom evalAngularIntegrals / unitarySpherePolynomials (libecp.c:278-292). */
+static int centre_build(const Sys *S, int C, Centre *cc, const double *radius, OracleStats *st) {
+  int O = S->small.order, nk = S->nk;
+  const double *x = S->small.x;
+  memset(cc, 0, sizeof *cc);
+  cc->C = C;
+  cc->L = S->ecpL[C];
+  for (int i = 0; i < 3; i++) cc->rC[i] = S->geom[3 * C + i];
+  int L = cc->L;
+  cc->utab = calloc((size_t)(L > 0 ? L : 1) * nk * O, sizeof(double));
+  cc->uL = calloc(O, sizeof(double));
+  double *Ul = calloc(O, sizeof(double));
+  int end = O - 1;
+  for (int l = 0; l < L; l++) {
+    for (int n = 0; n < O; n++) Ul[n] = eval_ecp(S, C, l, x[n], st);
+    end = potential_screen(0, end, Ul, 1.0E-14);
+    double *P = cc->utab + (size_t)l * nk * O;
+    for (int n = 0; n <= end; n++) {
+      P[n] = Ul[n];
+      for (int k = 1; k < nk; k++) P[k * O + n] = P[(k - 1) * O + n] * x[n];
+    }
+  }
+  cc->gridEnd = end;
+  for (int n = 0; n < O; n++) cc->uL[n] = eval_ecp(S, C, L, x[n], st);
+  free(Ul);
+
+  int ns = S->nShells;
+  cc->ws = calloc(ns + 1, sizeof(int));
+  cc->we = calloc(ns + 1, sizeof(int));
+  cc->skip = calloc(ns + 1, sizeof(int));
+  cc->F = calloc((size_t)(ns > 0 ? ns : 1) * nk * O, sizeof(double));
+  for (int sh = 0; sh < ns; sh++) {
+    double dAC = dist(cc->rC, S->geom + 3 * S->shAtom[sh]);
+    double R = radius[sh];
+    double rmin = dAC - R, rmax = dAC + R;
+    int j;
+    for (j = end; j >= 0; j--)
+      if (x[j] < rmin) break;
+    cc->ws[sh] = j + 1;
+    for (j = end; j >= 0; j--)
+      if (x[j] <= rmax) break;
+    cc->we[sh] = (j < 0 || x[j] > rmax) ? -1 : j;
+    cc->skip[sh] = !(cc->we[sh] >= cc->ws[sh]);
+  }
+  double K[64];
+  for (int sh = 0; sh < ns; sh++) {
+    if (cc->skip[sh]) continue;
+    double dAC = dist(cc->rC, S->geom + 3 * S->shAtom[sh]);
+    int lmaxA = S->maxLECP - 1 + S->lBS[sh];
+    double *Fs = cc->F + (size_t)sh * nk * O;
+    for (int pa = 0; pa < S->KBS[sh]; pa++) {
+      double zeta = S->aBS[S->shPrim[sh] + pa], da = S->dBS[S->shPrim[sh] + pa];
+      for (int n = cc->ws[sh]; n < cc->we[sh]; n++) {
+        bessel_eval(&S->bes, lmaxA, 2.0 * zeta * dAC * x[n], K, 1, st);
+        double e = dAC - x[n];
+        e = exp(-zeta * e * e);
+        st->exp_calls++;
+        st->table_points++;
+        for (int i = 0; i <= lmaxA; i++) Fs[i * O + n] += da * K[i] * e;
+      }
+    }
+  }
+
+  int na = S->nAtoms;
+  cc->omA = calloc(na, sizeof(double *));
+  cc->uspA = calloc(na, sizeof(double *));
+  cc->rAC = calloc(na, sizeof(double[3]));
+  cc->dAC = calloc(na, sizeof(double));
+  for (int A = 0; A < na; A++) {
+    const double *rA = S->geom + 3 * A;
+    cc->dAC[A] = dist(cc->rC, rA);
+    for (int i = 0; i < 3; i++) cc->rAC[A][i] = rA[i] - cc->rC[i];
+    cc->uspA[A] = usp_table(S->atomMaxL[A], cc->rAC[A]);
+    cc->omA[A] = angular_table(S, S->atomMaxL[A], cc->rAC[A]);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------ type 1 block */
+
+typedef struct {
+  double C, minExp;
+  const double *expo, *K, *U, *rn;
+} QCtx;
+
+static double q_integrand(int i, const void *vp) { /* src/type1.c:79-88 */
+  const QCtx *p = vp;
+  double e = p->expo[i];
+  return (e >= p->minExp) ? p->C * p->rn[i] * p->U[i] * p->K[i] * exp(e) : 0.0;
+}
+
+/* Radial Q[l1][l2] for one primitive pair, l2 = l1, l1-2, ...: PS93 on the
+ * pair's window of the small grid, then per failed (l1,l2) a PSM92 on the
+ * FM06-mapped large grid with the Gaussian prefactor regrouped;
+ * src/type1.c:95-208.  Buffers are shared between the two stages exactly as
+ * the reference shares them (small-grid rows stored with the small grid's
+ * stride), since the large-grid stage can read entries it did not write. */
+static int type1_Q(const Sys *S, const Centre *cc, double s, int lab, double dAC, double ca,
+                   double za, double dBC, double cb, double zb, int ws, int we, double *T,
+                   OracleStats *st) {
+  int Os = S->small.order, OL = S->large.order;
+  int Ob = OL > Os ? OL : Os;
+  double zd2 = -za * dAC * dAC - zb * dBC * dBC, z = -za - zb;
+  double *expo = calloc(Ob, sizeof(double)), *U = calloc(Ob, sizeof(double));
+  double *K = calloc((size_t)(lab + 1) * Ob, sizeof(double));
+  double *rn = calloc((size_t)(lab + 1) * Ob, sizeof(double));
+  int failed[256][2], nf = 0, status = 0;
+  const double *xs = S->small.x;
+  QCtx q;
+  q.C = ca * cb * exp(zd2);
+  q.minExp = S->lnAcc1;
+  q.expo = expo;
+  q.U = U;
+  st->t1_prim_pairs++;
+  for (int n = ws; n < we; n++) {
+    double r = xs[n];
+    expo[n] = (z * r + s) * r;
+    U[n] = cc->uL[n];
+    bessel_eval(&S->bes, lab, s * r, K + n, Os, st);
+    st->table_points++;
+    rn[n] = 1.0;
+    for (int l1 = 1; l1 <= lab; l1++) rn[l1 * Os + n] = r * rn[(l1 - 1) * Os + n];
+  }
+  for (int l1 = 0; l1 <= lab; l1++) {
+    q.rn = rn + l1 * Os;
+    for (int l2 = l1; l2 >= 0; l2 -= 2) {
+      double I;
+      q.K = K + l2 * Os;
+      if (quad_ps93(&S->small.sch, S->small.w, ws, we, S->tol, q_integrand, &q, &I, st)) {
+        failed[nf][0] = l1;
+        failed[nf][1] = l2;
+        nf++;
+      } else {
+        T[l1 * (lab + 1) + l2] += I;
+      }
+    }
+  }
+  if (nf > 0) {
+    st->t1_fallback_pp++;
+    double *x = malloc(OL * sizeof(double)), *w = malloc(OL * sizeof(double));
+    double zp = za + zb, P = (za * dAC + zb * dBC) / zp;
+    int end = OL - 1;
+    map_fm06(OL, S->large.x, S->large.w, x, w, zp, P);
+    q.C = ca * cb;
+    for (int n = 0; n < OL; n++) {
+      double r = x[n];
+      expo[n] = (z * r + s) * r + zd2;
+      if (r > dAC && r > dBC && expo[n] < q.minExp) {
+        end = n - 1;
+        break;
+      } else if (expo[n] >= q.minExp) {
+        bessel_eval(&S->bes, lab, s * r, K + n, OL, st);
+        st->table_points++;
+        U[n] = eval_ecp(S, cc->C, cc->L, r, st);
+        rn[n] = 1.0;
+        for (int l1 = 1; l1 <= lab; l1++) rn[l1 * OL + n] = r * rn[(l1 - 1) * OL + n];
+      }
+    }
+    if (end < S->large.sch.head[0]) st->stale_reads += nf;
+    for (int k = 0; k < nf; k++) {
+      double I;
+      q.rn = rn + failed[k][0] * OL;
+      q.K = K + failed[k][1] * OL;
+      if (quad_psm92(&S->large.sch, w, 0, end, S->tol, q_integrand, &q, &I, st)) {
+        status = 1;
+        break;
+      }
+      T[failed[k][0] * (lab + 1) + failed[k][1]] += I;
+    }
+    free(x);
+    free(w);
+  }
+  free(expo); free(U); free(K); free(rn);
+  return status;
+}
+
+/* chi[Cart a][Cart b] (running indices up to la, lb): sum over primitive
+ * pairs of S_lm(P) x poly2sph x Q; src/type1.c:212-302. */
+static int type1_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, int we,
+                       double *chi, OracleStats *st) {
+  int A = S->shAtom[sa], B = S->shAtom[sb];
+  int la = S->lBS[sa], lb = S->lBS[sb], lab = la + lb;
+  int d = S->ijkDim, tmW = NSPH(S->tmDim), inc = NCUM(lb);
+  const double *rAC = cc->rAC[A], *rBC = cc->rAC[B];
+  double dAC = cc->dAC[A], dBC = cc->dAC[B];
+  double rsh[400], Q[400];
+  for (int pa = 0; pa < S->KBS[sa]; pa++) {
+    double za = S->aBS[S->shPrim[sa] + pa], ca = S->dBS[S->shPrim[sa] + pa];
+    for (int pb = 0; pb < S->KBS[sb]; pb++) {
+      double zb = S->aBS[S->shPrim[sb] + pb], cb = S->dBS[S->shPrim[sb] + pb];
+      double P[3], Sp[3];
+      for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * rAC[i] + zb * rBC[i]);
+      to_spherical(P, Sp);
+      real_sph(lab, Sp[1], Sp[2], S->fac, S->dfac, rsh);
+      memset(Q, 0, (lab + 1) * (lab + 1) * sizeof(double));
+      if (type1_Q(S, cc, Sp[0], lab, dAC, ca, za, dBC, cb, zb, ws, we, Q, st)) return 1;
+      for (int ax = 0; ax <= la; ax++)
+        for (int ay = 0; ay <= la - ax; ay++)
+          for (int az = 0; az <= la - ax - ay; az++) {
+            int i = S->ijkIdx[(ax * d + ay) * d + az];
+            for (int bx = 0; bx <= lb; bx++)
+              for (int by = 0; by <= lb - bx; by++)
+                for (int bz = 0; bz <= lb - bx - by; bz++) {
+                  int j = S->ijkIdx[(bx * d + by) * d + bz];
+                  int lx = ax + bx, ly = ay + by, lz = az + bz, lmax = lx + ly + lz;
+                  int p = S->ijkIdx[(lx * d + ly) * d + lz];
+                  for (int l = lmax; l >= 0; l -= 2) {
+                    double factor = 0.0;
+                    for (int m = 0; m < 2 * l + 1; m++)
+                      factor += rsh[LM(l, m)] * S->p2s[(size_t)p * tmW + LM(l, m)];
+                    chi[i * inc + j] += factor * Q[lmax * (lab + 1) + l];
+                    st->contraction_fma += 2 * l + 2;
+                  }
+                }
+          }
+    }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------ type 2 block */
+
+typedef struct {
+  const double *Fa, *Fb, *U;
+} TCtx;
+
+static double t_integrand(int i, const void *vp) { /* src/type2.c:320-322 */
+  const TCtx *p = vp;
+  return p->Fa[i] * p->Fb[i] * p->U[i];
+}
+
+typedef struct {
+  double C, minExp;
+  const double *expo, *Ka, *Kb, *U, *rn;
+} QFCtx;
+
+static double qf_integrand(int i, const void *vp) { /* src/type2.c:398-410 */
+  const QFCtx *p = vp;
+  double e = p->expo[i];
+  return (e >= p->minExp) ? p->C * p->U[i] * p->rn[i] * p->Ka[i] * p->Kb[i] * exp(e) : 0.0;
+}
+
+/* Per failed (l1,l2,l3): sum over primitive pairs of PSM92 on the pair's
+ * FM06-mapped 1023-point grid; buffers persist across primitive pairs
+ * (src/type2.c:418-528), so entries beyond a pair's screened end keep the
+ * previous pair's values -- reproduced here because the lower half of the
+ * grid is always integrated. */
+static int type2_fallback(const Sys *S, const Centre *cc, int l, int sa, int sb, int la, int lb,
+                          double dAC, double dBC, const int (*fl)[3], int nf, double *T,
+                          OracleStats *st) {
+  int OL = S->large.order, laC = la + l, lbC = lb + l, lab = la + lb;
+  int ti1 = (lbC + 1) * (lab + 1), ti2 = lab + 1;
+  double *expo = calloc(OL, sizeof(double)), *U = calloc(OL, sizeof(double));
+  double *Ka = calloc((size_t)(laC + 1) * OL, sizeof(double));
+  double *Kb = calloc((size_t)(lbC + 1) * OL, sizeof(double));
+  double *rn = calloc((size_t)(lab + 1) * OL, sizeof(double));
+  double *x = malloc(OL * sizeof(double)), *w = malloc(OL * sizeof(double));
+  int status = 0;
+  QFCtx q;
+  q.minExp = S->lnAcc2;
+  q.expo = expo;
+  q.U = U;
+  for (int pa = 0; pa < S->KBS[sa] && !status; pa++) {
+    double za = S->aBS[S->shPrim[sa] + pa], ca = S->dBS[S->shPrim[sa] + pa];
+    double s1 = 2.0 * za * dAC;
+    for (int pb = 0; pb < S->KBS[sb]; pb++) {
+      double zb = S->aBS[S->shPrim[sb] + pb], cb = S->dBS[S->shPrim[sb] + pb];
+      double s2 = 2.0 * zb * dBC, zp = za + zb, P = (za * dAC + zb * dBC) / zp;
+      int end = OL - 1;
+      st->t2_fallback_pp++;
+      q.C = ca * cb;
+      map_fm06(OL, S->large.x, S->large.w, x, w, zp, P);
+      for (int n = 0; n < OL; n++) {
+        double r = x[n], d1 = dAC - r, d2 = dBC - r;
+        expo[n] = -za * d1 * d1 - zb * d2 * d2;
+        if (r > dAC && r > dBC && expo[n] < q.minExp) {
+          end = n - 1;
+          break;
+        } else if (expo[n] >= q.minExp) {
+          U[n] = eval_ecp(S, cc->C, l, r, st);
+          bessel_eval(&S->bes, laC, s1 * r, Ka + n, OL, st);
+          bessel_eval(&S->bes, lbC, s2 * r, Kb + n, OL, st);
+          st->table_points++;
+          rn[n] = 1.0;
+          for (int k = 1; k <= lab; k++) rn[k * OL + n] = r * rn[(k - 1) * OL + n];
+        }
+      }
+      if (end < S->large.sch.head[0]) st->stale_reads += nf;
+      for (int f = nf - 1; f >= 0; f--) {
+        double I;
+        q.Ka = Ka + fl[f][0] * OL;
+        q.Kb = Kb + fl[f][1] * OL;
+        q.rn = rn + fl[f][2] * OL;
+        if (quad_psm92(&S->large.sch, w, 0, end, S->tol, qf_integrand, &q, &I, st)) {
+          status = 1;
+          break;
+        }
+        T[fl[f][0] * ti1 + fl[f][1] * ti2 + fl[f][2]] += I;
+      }
+      if (status) break;
+    }
+  }
+  free(expo); free(U); free(Ka); free(Kb); free(rn); free(x); free(w);
+  return status;
+}
+
+/* gamma[Cart a][Cart b] = sum_l sum_{lambda1,lambda2}
+ *   (sum_m OmegaA OmegaB) T[lambda1][lambda2][alpha+beta];
+ * src/type2.c:533-631 with calcT_fast_FM06 (:337-387). */
+static int type2_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, int we,
+                       double *gam, OracleStats *st) {
+  int A = S->shAtom[sa], B = S->shAtom[sb];
+  int la = S->lBS[sa], lb = S->lBS[sb], lab = la + lb, O = S->small.order, nk = S->nk;
+  int inc = NCUM(lb);
+  int aI1 = NCUM(S->atomMaxL[A]), aI2 = S->omD1 * aI1;
+  int bI1 = NCUM(S->atomMaxL[B]), bI2 = S->omD1 * bI1;
+  const double *omA = cc->omA[A], *omB = cc->omA[B];
+  const double *Fa = cc->F + (size_t)sa * nk * O, *Fb = cc->F + (size_t)sb * nk * O;
+  double dAC = cc->dAC[A], dBC = cc->dAC[B];
+  for (int l = 0; l < cc->L; l++) {
+    int n1 = la + l + 1, n2 = lb + l + 1, n3 = lab + 1;
+    double *T = calloc((size_t)n1 * n2 * n3, sizeof(double));
+    int (*fl)[3] = malloc(sizeof(int[3]) * n1 * n2 * n3);
+    int nf = 0;
+    TCtx t;
+    st->t2_items++;
+    for (int l1 = 0; l1 < n1; l1++) {
+      t.Fa = Fa + l1 * O;
+      for (int l2 = 0; l2 < n2; l2++) {
+        t.Fb = Fb + l2 * O;
+        for (int l3 = 0; l3 < n3; l3++) {
+          double I;
+          t.U = cc->utab + ((size_t)l * nk + l3) * O;
+          if (quad_ps93(&S->small.sch, S->small.w, ws, we, S->tol, t_integrand, &t, &I, st)) {
+            fl[nf][0] = l1; fl[nf][1] = l2; fl[nf][2] = l3;
+            nf++;
+          } else {
+            T[(l1 * n2 + l2) * n3 + l3] = I;
+          }
+        }
+      }
+    }
+    if (nf > 0) {
+      st->t2_fallback_items++;
+      if (type2_fallback(S, cc, l, sa, sb, la, lb, dAC, dBC, (const int(*)[3])fl, nf, T, st)) {
+        free(T); free(fl);
+        return 2;
+      }
+    }
+    for (int alpha = 0; alpha <= la; alpha++) {
+      int par = (alpha + l) % 2, ll1 = l - alpha;
+      ll1 = par > ll1 ? par : ll1;
+      for (int c1 = 0; c1 < NCART(alpha); c1++) {
+        int p = NCUM(alpha - 1) + c1;
+        for (int beta = 0; beta <= lb; beta++) {
+          int ab = alpha + beta, par2 = (beta + l) % 2, ll2 = l - beta;
+          ll2 = par2 > ll2 ? par2 : ll2;
+          for (int c2 = 0; c2 < NCART(beta); c2++) {
+            int q = NCUM(beta - 1) + c2;
+            double tmp = 0.0;
+            for (int l1 = ll1; l1 <= la + l; l1 += 2)
+              for (int l2 = ll2; l2 <= lb + l; l2 += 2) {
+                double factor = 0.0;
+                for (int m = 0; m < 2 * l + 1; m++)
+                  factor += omA[l1 * aI2 + LM(l, m) * aI1 + p] * omB[l2 * bI2 + LM(l, m) * bI1 + q];
+                tmp += factor * T[(l1 * n2 + l2) * n3 + ab];
+                st->contraction_fma += 2 * l + 2;
+              }
+            gam[p * inc + q] += tmp;
+          }
+        }
+      }
+    }
+    free(T);
+    free(fl);
+  }
+  return 0;
+}
+
+/* Binomial re-centring of the C-centred block onto A and B, times `norm`;
+ * src/util.c:247-334.  gam is NCUM(la) x NCUM(lb), out NCART(la) x NCART(lb). */
+static void poly_shift(const Sys *S, const double *gam, int la, const double *uspA, int dA,
+                       int lb, const double *uspB, int dB, double norm, double *out,
+                       OracleStats *st) {
+  int d = S->ijkDim, incG = NCUM(lb), incJ = NCUM(lb), incI = NCART(lb);
+  const double *fac = S->fac;
+  double *J = calloc((size_t)NCART(la) * NCUM(lb), sizeof(double));
+  memset(out, 0, sizeof(double) * NCART(la) * NCART(lb));
+  for (int c1 = 0; c1 < NCART(la); c1++) {
+    const int *e = S->ijk + 3 * (NCUM(la - 1) + c1);
+    for (int x = 0; x <= e[0]; x++) {
+      double bx = binom(e[0], x, fac);
+      for (int y = 0; y <= e[1]; y++) {
+        double by = bx * binom(e[1], y, fac);
+        for (int z = 0; z <= e[2]; z++) {
+          double bz = by * binom(e[2], z, fac);
+          double factor = bz * uspA[((e[0] - x) * dA + (e[1] - y)) * dA + (e[2] - z)];
+          if (fabs(factor) <= S->acc) continue;
+          int r = S->ijkIdx[(x * d + y) * d + z];
+          for (int q = 0; q < NCUM(lb); q++) J[c1 * incJ + q] += factor * gam[r * incG + q];
+          st->contraction_fma += NCUM(lb);
+        }
+      }
+    }
+  }
+  for (int c2 = 0; c2 < NCART(lb); c2++) {
+    const int *e = S->ijk + 3 * (NCUM(lb - 1) + c2);
+    for (int x = 0; x <= e[0]; x++) {
+      double bx = binom(e[0], x, fac);
+      for (int y = 0; y <= e[1]; y++) {
+        double by = bx * binom(e[1], y, fac);
+        for (int z = 0; z <= e[2]; z++) {
+          double bz = by * binom(e[2], z, fac);
+          double factor = bz * uspB[((e[0] - x) * dB + (e[1] - y)) * dB + (e[2] - z)];
+          if (fabs(factor) <= S->acc) continue;
+          factor *= norm;
+          int r = S->ijkIdx[(x * d + y) * d + z];
+          for (int c1 = 0; c1 < NCART(la); c1++) out[c1 * incI + c2] += factor * J[c1 * incJ + r];
+          st->contraction_fma += NCART(la);
+        }
+      }
+    }
+  }
+  free(J);
+}
+
+/* ------------------------------------------------------------- the driver */
+
+typedef struct {
+  /* getIntegrals-style accumulation */
+  double *I;
+  int rowdim;
+  /* block recording */
+  int maxBlocks, nBlocks;
+  int *meta;
+  long long maxData, nData;
+  double *data;
+  int overflow;
+} Sink;
+
+static void emit(const Sys *S, Sink *k, int C, int sa, int sb, int type, const double *blk) {
+  int la = S->lBS[sa], lb = S->lBS[sb], na = NCART(la), nb = NCART(lb);
+  if (k->I) { /* libECP_callback0, src/getIntegrals.c:23-43 */
+    int a0 = S->shAO[sa], b0 = S->shAO[sb];
+    for (int i = 0; i < na; i++)
+      for (int j = 0; j < nb; j++)
+        if (a0 + i <= b0 + j) k->I[(size_t)(a0 + i) * k->rowdim + b0 + j] += blk[i * nb + j];
+  }
+  if (k->meta) {
+    if (k->nBlocks >= k->maxBlocks || k->nData + na * nb > k->maxData) { k->overflow = 1; return; }
+    int A = S->shAtom[sa], B = S->shAtom[sb];
+    int *m = k->meta + 8 * k->nBlocks;
+    m[0] = A; m[1] = sa - S->atomShell0[A]; m[2] = la;
+    m[3] = B; m[4] = sb - S->atomShell0[B]; m[5] = lb;
+    m[6] = C; m[7] = type;
+    memcpy(k->data + k->nData, blk, sizeof(double) * na * nb);
+    k->nData += na * nb;
+    k->nBlocks++;
+  }
+}
+
+/* The C -> A -> B>=A -> s1 -> s2 loop of calculateECPIntegrals
+ * (src/libecp.c:213-404) for one ECP centre. */
+static int run_centre(const Sys *S, int C, const double *radius, Sink *k, OracleStats *st) {
+  Centre cc;
+  centre_build(S, C, &cc, radius, st);
+  int lmaxBS = S->maxLBS;
+  double *chi = malloc(sizeof(double) * NCUM(lmaxBS) * NCUM(lmaxBS));
+  double *blk = malloc(sizeof(double) * NCART(lmaxBS) * NCART(lmaxBS));
+  int status = 0;
+  for (int A = 0; A < S->nAtoms && !status; A++)
+    for (int B = A; B < S->nAtoms && !status; B++)
+      for (int i = 0; i < S->atomNShell[A] && !status; i++)
+        for (int j = 0; j < S->atomNShell[B]; j++) {
+          int sa = S->atomShell0[A] + i, sb = S->atomShell0[B] + j;
+          if ((A == B && j < i) || cc.skip[sa] || cc.skip[sb]) continue;
+          int ws = cc.ws[sa] > cc.ws[sb] ? cc.ws[sa] : cc.ws[sb];
+          int we = cc.we[sa] > cc.we[sb] ? cc.we[sa] : cc.we[sb];
+          if (!(ws < we)) continue;
+          int la = S->lBS[sa], lb = S->lBS[sb];
+          int dA = S->atomMaxL[A] + 1, dB = S->atomMaxL[B] + 1;
+          const double norm1 = 4.0 * kPi, norm2 = norm1 * norm1;
+          st->blocks++;
+          memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
+          if (type1_block(S, &cc, sa, sb, ws, we, chi, st)) { status = 2; break; }
+          poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm1, blk, st);
+          emit(S, k, C, sa, sb, 1, blk);
+          memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
+          if (type2_block(S, &cc, sa, sb, ws, we, chi, st)) { status = 2; break; }
+          poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm2, blk, st);
+          emit(S, k, C, sa, sb, 2, blk);
+        }
+  free(chi);
+  free(blk);
+  centre_free(&cc, S->nAtoms);
+  return status;
+}
+
+static double *radii(const Sys *S, int *bad) {
+  double *r = calloc(S->nShells + 1, sizeof(double));
+  *bad = 0;
+  for (int s = 0; s < S->nShells; s++) {
+    r[s] = shell_radius(S, s);
+    if (r[s] < 0) *bad = 1;
+  }
+  return r;
+}
+
+#define SYS_ARGS                                                                          \
+  int nrAtoms, const double *geometry, const int *shellsECP, const int *KECP,             \
+      const int *lECP, const double *nECP, const double *dECP, const double *aECP,        \
+      const int *shellsBS, const int *lBS, const int *KBS, const double *dBS,             \
+      const double *aBS, int largeGridOrder, double tolerance, double accuracy
+#define SYS_PASS                                                                          \
+  nrAtoms, geometry, shellsECP, KECP, lECP, nECP, dECP, aECP, shellsBS, lBS, KBS, dBS,    \
+      aBS, largeGridOrder, tolerance, accuracy
+
+static int run(SYS_ARGS, int centerLo, int centerHi, const unsigned char *mask, Sink *k,
+               OracleStats *stats) {
+  Sys S;
+  OracleStats local;
+  memset(&local, 0, sizeof local);
+  int st = sys_build(&S, SYS_PASS);
+  if (st) { sys_free(&S); return st; }
+  int bad;
+  double *rad = radii(&S, &bad);
+  if (bad) st = 1;
+  for (int C = centerLo; C < centerHi && C < nrAtoms && !st; C++) {
+    if (S.ecpL[C] < 0 || (mask && !mask[C])) continue;
+    st = run_centre(&S, C, rad, k, &local);
+  }
+  free(rad);
+  sys_free(&S);
+  if (stats) {
+    long long *a = (long long *)stats, *b = (long long *)&local;
+    for (size_t i = 0; i < sizeof(OracleStats) / sizeof(long long); i++) a[i] += b[i];
+  }
+  return st;
+}
+
+int oracle_getIntegrals(SYS_ARGS, int rowdim, double *I, int centerLo, int centerHi,
+                        OracleStats *stats) {
+  Sink k;
+  memset(&k, 0, sizeof k);
+  k.I = I;
+  k.rowdim = rowdim;
+  return run(SYS_PASS, centerLo, centerHi, NULL, &k, stats);
+}
+
+int oracle_blocks(SYS_ARGS, int centerLo, int centerHi, int maxBlocks, int *meta,
+                  long long maxData, double *data, int *nBlocks, long long *nData,
+                  OracleStats *stats) {
+  Sink k;
+  memset(&k, 0, sizeof k);
+  k.maxBlocks = maxBlocks; k.meta = meta; k.maxData = maxData; k.data = data;
+  int st = run(SYS_PASS, centerLo, centerHi, NULL, &k, stats);
+  *nBlocks = k.nBlocks;
+  *nData = k.nData;
+  if (k.overflow) return -2;
+  return st;
+}
+
+typedef struct {
+  int nrAtoms;
+  const double *geometry;
+  const int *shellsECP, *KECP, *lECP;
+  const double *nECP, *dECP, *aECP;
+  const int *shellsBS, *lBS, *KBS;
+  const double *dBS, *aBS;
+  int largeGridOrder;
+  double tolerance, accuracy;
+  int dim, status;
+  unsigned char *mask;
+  double *I;
+  OracleStats st;
+} Job;
+
+static void *job_main(void *vp) {
+  Job *j = vp;
+  Sink k;
+  memset(&k, 0, sizeof k);
+  k.I = j->I;
+  k.rowdim = j->dim;
+  memset(&j->st, 0, sizeof j->st);
+  j->status = run(j->nrAtoms, j->geometry, j->shellsECP, j->KECP, j->lECP, j->nECP, j->dECP,
+                  j->aECP, j->shellsBS, j->lBS, j->KBS, j->dBS, j->aBS, j->largeGridOrder,
+                  j->tolerance, j->accuracy, 0, j->nrAtoms, j->mask, &k, &j->st);
+  return NULL;
+}
+
+int oracle_getIntegrals_mt(SYS_ARGS, int rowdim, double *I, int nThreads, OracleStats *stats) {
+  int ns = 0, dim = 0, nc = 0;
+  for (int i = 0; i < nrAtoms; i++) ns += shellsBS[i];
+  for (int s = 0; s < ns; s++) dim += NCART(lBS[s]);
+  for (int i = 0; i < nrAtoms; i++) nc += shellsECP[i] > 0;
+  if (nThreads > nc) nThreads = nc;
+  if (nThreads < 1) nThreads = 1;
+  Job *jobs = calloc(nThreads, sizeof(Job));
+  pthread_t *th = calloc(nThreads, sizeof(pthread_t));
+  int status = 0, c = 0;
+  for (int t = 0; t < nThreads; t++) {
+    Job *j = &jobs[t];
+    j->nrAtoms = nrAtoms; j->geometry = geometry; j->shellsECP = shellsECP; j->KECP = KECP;
+    j->lECP = lECP; j->nECP = nECP; j->dECP = dECP; j->aECP = aECP; j->shellsBS = shellsBS;
+    j->lBS = lBS; j->KBS = KBS; j->dBS = dBS; j->aBS = aBS;
+    j->largeGridOrder = largeGridOrder; j->tolerance = tolerance; j->accuracy = accuracy;
+    j->dim = dim > 0 ? dim : 1;
+    j->I = calloc((size_t)j->dim * j->dim, sizeof(double));
+    j->mask = calloc(nrAtoms + 1, 1);
+  }
+  /* ECP centres are dealt round-robin: the t-th, (t+n)-th, ... go to thread t */
+  for (int i = 0; i < nrAtoms; i++)
+    if (shellsECP[i] > 0) jobs[(c++) % nThreads].mask[i] = 1;
+  for (int t = 0; t < nThreads; t++) pthread_create(&th[t], NULL, job_main, &jobs[t]);
+  for (int t = 0; t < nThreads; t++) pthread_join(th[t], NULL);
+  for (int t = 0; t < nThreads; t++) {
+    if (jobs[t].status) status = jobs[t].status;
+    for (int i = 0; i < dim; i++)
+      for (int j = i; j < dim; j++) I[(size_t)i * rowdim + j] += jobs[t].I[(size_t)i * jobs[t].dim + j];
+    if (stats) {
+      long long *a = (long long *)stats, *b = (long long *)&jobs[t].st;
+      for (size_t i = 0; i < sizeof(OracleStats) / sizeof(long long); i++) a[i] += b[i];
+    }
+    free(jobs[t].I);
+    free(jobs[t].mask);
+  }
+  free(jobs);
+  free(th);
+  return status;
+}
+
+/* ------------------------------------------------------------ test probes */
+
+int oracle_grid(int which, int maxPoints, double *x, double *w) {
+  Grid g;
+  if (which == 0) grid_ps93(&g, maxPoints, 0.0);
+  else grid_psm92(&g, maxPoints, 0.0);
+  memcpy(x, g.x, g.order * sizeof(double));
+  memcpy(w, g.w, g.order * sizeof(double));
+  int n = g.order;
+  free(g.x); free(g.w); free(g.sch.idx);
+  return n;
+}
+
+int oracle_bessel(int lmax, double z, int tabLmax, double accuracy, double *K) {
+  Bessel b;
+  OracleStats st;
+  if (bessel_table(&b, tabLmax, 1600, 200, accuracy)) return 1;
+  bessel_eval(&b, lmax, z, K, 1, &st);
+  free(b.K); free(b.C);
+  return 0;
+}
+
+int oracle_rsh(int lmax, double theta, double phi, double *out) {
+  double *fac = fact_table(2 * lmax + 4, 1, 0), *dfac = fact_table(2 * lmax + 4, 2, 0);
+  real_sph(lmax, theta, phi, fac, dfac, out);
+  free(fac); free(dfac);
+  return 0;
+}
