@@ -1,0 +1,55 @@
+/*
+ * libecp.h -- handle interface of the drop-in library (replaces chrr/libECP
+ * src/libecp.h:6-29; same symbols, argument order and semantics).
+ *
+ * libECP_init keeps the caller's geometry and basis arrays by pointer (they
+ * must outlive the handle) and copies the ECP terms (src/libecp.c:68-127).
+ * calculateECPIntegrals computes every (shell pair, ECP centre) block on the
+ * GPU, then hands the blocks to the callback in the reference's order
+ * (centre C, atom A, atom B >= A, shell s1 of A, shell s2 of B -- s2 >= s1 when
+ * A == B -- type-1 block then type-2 block), each IJK(la) x IJK(lb) row-major
+ * in libint Cartesian order and freed after the callback returns
+ * (src/libecp.c:256-397).  Return value: 0 ok, 1 a type-1 large-grid
+ * quadrature did not converge, 2 a type-2 one did not; callbacks stop at the
+ * failing block, as the reference's control flow does.
+ */
+#ifndef LIBECP_H
+#define LIBECP_H 1
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct _libECPHandle libECPHandle;
+
+/* The reference's typedef names the parameters (A, B, C, sa, sb, la, lb,
+ * shifta, shiftb, I, p) but calls it as below (src/libecp.c:372,
+ * src/getIntegrals.c:23-25); the ABI is the same nine ints, a double* and a
+ * void*, and the meaning follows the call site. */
+typedef void (*ECPCallback)(int A, int sa, int la, int shifta,
+                            int B, int sb, int lb, int shiftb,
+                            int C, double *I, void *p);
+
+/* The reference's header names parameters 4 and 5 (KECP, lECP) but its
+ * definition reads them as (lECP, KECP) (src/libecp.c:55), and getIntegrals
+ * passes them in that order; this declaration follows the definition.
+ * n: derivative order (0 only in this library -- other values return NULL).
+ * lmax / shellOrdering: custom Cartesian ordering (NULL = libint default; a
+ * custom ordering returns NULL in this library).
+ * Returns NULL on failure. */
+libECPHandle *libECP_init(int nrAtoms, double *geometry,
+                          int *shellsECP, int *lECP, int *KECP,
+                          double *nECP, double *dECP, double *aECP,
+                          int *shellsBS, int *lBS, int *KBS,
+                          double *dBS, double *aBS,
+                          int n, int lmax, int *shellOrdering,
+                          int largeGridOrder, double tolerance, double accuracy);
+
+int calculateECPIntegrals(libECPHandle *h, ECPCallback cb, void *args);
+
+void libECP_free(libECPHandle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIBECP_H */

@@ -1,0 +1,96 @@
+/*
+ * libecp_gb300.h -- entry points beside the drop-in interface.
+ *
+ * These have no counterpart in chrr/libECP; they expose what the GPU engine
+ * adds: every block at once with a per-unit status, a device-resident job
+ * that can be re-run without host traffic (benchmarks, serving), and the
+ * pipe-throughput probe the roofline figures are quoted against.
+ *
+ * A "unit" is one (shell pair, ECP centre) combination.  Units are numbered
+ * u = c * nPairs + p, c the rank of the ECP centre among atoms with an ECP,
+ * p the rank of the shell pair in the reference's loop order (atom A, atom
+ * B >= A, shell s1 of A, shell s2 of B, s2 >= s1 when A == B).  Each unit owns
+ * two blocks (type 1 then type 2) of IJK(la) x IJK(lb) doubles.
+ */
+#ifndef LIBECP_GB300_H
+#define LIBECP_GB300_H 1
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The arrays of getIntegrals (src/getIntegrals.h:7-13) in one struct. */
+typedef struct {
+  int nrAtoms;
+  const double *geometry;
+  const int *shellsECP, *KECP, *lECP;
+  const double *nECP, *dECP, *aECP;
+  const int *shellsBS, *lBS, *KBS;
+  const double *dBS, *aBS;
+  int largeGridOrder;
+  double tolerance, accuracy;
+} ecpgb_system;
+
+enum {
+  ECPGB_FP64 = 0,   /* plain FP64 kernels, one unit per CTA (the drop-in path) */
+};
+
+enum {
+  ECPGB_UNIT_DONE = 0,
+  ECPGB_UNIT_SKIPPED = 1,     /* screened out: no callback in the reference   */
+  ECPGB_UNIT_FAIL_TYPE1 = 2,  /* type-1 large-grid quadrature not converged   */
+  ECPGB_UNIT_FAIL_TYPE2 = 3,  /* type-2 large-grid quadrature not converged   */
+};
+
+typedef struct {
+  long long units;        /* (pair, centre) units                        */
+  long long emitted;      /* units that produced blocks                  */
+  long long firstFailed;  /* first failing unit, -1 if none              */
+  long long values;       /* doubles in the block layout                 */
+  double msGpu;           /* device time of the last run (CUDA events)   */
+  double msUnitKernel;    /* of which the per-unit kernel                */
+  long long h2dBytes, d2hBytes;
+} ecpgb_info;
+
+/* Sizes of the block layout: units and doubles.  0 ok. */
+int ecpgb_layout(const ecpgb_system *s, long long *nUnits, long long *nValues);
+
+/* All blocks.  values[nValues] receives unit u's two blocks at
+ * offsets[u] (type 1) and offsets[u] + IJK(la)*IJK(lb) (type 2); status[u]
+ * one of ECPGB_UNIT_*.  offsets / status may be NULL.  0 ok, nonzero on set-up
+ * errors (see ecpgb_last_error). */
+int ecpgb_blocks(const ecpgb_system *s, int mode, double *values, long long *offsets,
+                 int *status, ecpgb_info *info);
+
+/* getIntegrals with a precision mode, a status and timings: returns 0 ok,
+ * 1 set-up failed, 2 a large-grid quadrature did not converge (the matrix then
+ * holds every block before the failing one, in the reference's order). */
+int ecpgb_getIntegrals(const ecpgb_system *s, int mode, int rowdim, double *I,
+                       ecpgb_info *info);
+
+/* Device-resident job: inputs are copied to HBM once; ecpgb_job_run then
+ * re-runs the whole pipeline (all kernels) nRuns times without host traffic,
+ * writing one device-time per run (CUDA events on the engine's stream) to
+ * msRun and the per-unit kernel's time to msUnit (either may be NULL).  With
+ * flushL2 != 0 a 256 MiB buffer is written between runs, outside the timed
+ * spans, so no run starts with a warm L2. */
+typedef struct ecpgb_job ecpgb_job;
+ecpgb_job *ecpgb_job_create(const ecpgb_system *s, int mode);
+int ecpgb_job_run(ecpgb_job *j, int nRuns, int flushL2, float *msRun, float *msUnit);
+int ecpgb_job_matrix(ecpgb_job *j, int rowdim, double *I); /* += last run's matrix */
+long long ecpgb_job_units(const ecpgb_job *j, long long *emitted);
+int ecpgb_job_kernel_launches(const ecpgb_job *j);           /* kernels per run */
+void ecpgb_job_free(ecpgb_job *j);
+
+/* Pipe-throughput probe on the current device: out[0] FP64 FMA TFLOP/s,
+ * out[1] FP32 FMA TFLOP/s, out[2] MUFU ex2 Gop/s, out[3] FP64 exp() Gop/s.
+ * Takes about 0.5 s.  0 ok. */
+int ecpgb_measure_peaks(double *out);
+
+/* Text of the last error on this thread ("" if none). */
+const char *ecpgb_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIBECP_GB300_H */

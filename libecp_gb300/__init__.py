@@ -1,0 +1,273 @@
+"""libecp_gb300 -- GB300-native ECP integral engine behind libECP's C interface.
+
+The product is the shared library ``libecp_gb300.so`` (CUDA kernels for
+sm_103a plus the C ABI declared in ``include/``).  This module is a thin ctypes
+view of that library for Python callers, tests and the benchmark; it performs
+no arithmetic of its own, and it raises if the library has not been built --
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+import numpy as np
+
+from .workloads import EcpSystem, ncart  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libecp_gb300.so")
+
+_D = ct.POINTER(ct.c_double)
+_I = ct.POINTER(ct.c_int)
+_LL = ct.POINTER(ct.c_longlong)
+_F = ct.POINTER(ct.c_float)
+
+ECPGB_FP64 = 0
+UNIT_DONE, UNIT_SKIPPED, UNIT_FAIL_TYPE1, UNIT_FAIL_TYPE2 = 0, 1, 2, 3
+
+
+class EcpgbSystem(ct.Structure):
+    _fields_ = [("nrAtoms", ct.c_int), ("geometry", _D), ("shellsECP", _I), ("KECP", _I),
+                ("lECP", _I), ("nECP", _D), ("dECP", _D), ("aECP", _D), ("shellsBS", _I),
+                ("lBS", _I), ("KBS", _I), ("dBS", _D), ("aBS", _D), ("largeGridOrder", ct.c_int),
+                ("tolerance", ct.c_double), ("accuracy", ct.c_double)]
+
+
+class EcpgbInfo(ct.Structure):
+    _fields_ = [("units", ct.c_longlong), ("emitted", ct.c_longlong),
+                ("firstFailed", ct.c_longlong), ("values", ct.c_longlong),
+                ("msGpu", ct.c_double), ("msUnitKernel", ct.c_double),
+                ("h2dBytes", ct.c_longlong), ("d2hBytes", ct.c_longlong)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+ECP_CALLBACK = ct.CFUNCTYPE(None, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
+                            ct.c_int, ct.c_int, ct.c_int, _D, ct.c_void_p)
+
+_lib = None
+
+
+def lib() -> ct.CDLL:
+    """The loaded C-ABI library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -m libecp_gb300.build` "
+            "(the ECP engine has no CPU fallback)")
+    L = ct.CDLL(LIB_PATH)
+    sys_args = [ct.c_int, _D, _I, _I, _I, _D, _D, _D, _I, _I, _I, _D, _D, ct.c_int, ct.c_double,
+                ct.c_double]
+    L.getIntegrals.argtypes = sys_args + [ct.c_int, _D]
+    L.getIntegrals.restype = ct.c_int
+    L.libECP_init.argtypes = [ct.c_int, _D, _I, _I, _I, _D, _D, _D, _I, _I, _I, _D, _D, ct.c_int,
+                              ct.c_int, _I, ct.c_int, ct.c_double, ct.c_double]
+    L.libECP_init.restype = ct.c_void_p
+    L.calculateECPIntegrals.argtypes = [ct.c_void_p, ECP_CALLBACK, ct.c_void_p]
+    L.calculateECPIntegrals.restype = ct.c_int
+    L.libECP_free.argtypes = [ct.c_void_p]
+    L.libECP_free.restype = None
+    P = ct.POINTER(EcpgbSystem)
+    L.ecpgb_layout.argtypes = [P, _LL, _LL]
+    L.ecpgb_blocks.argtypes = [P, ct.c_int, _D, _LL, _I, ct.POINTER(EcpgbInfo)]
+    L.ecpgb_getIntegrals.argtypes = [P, ct.c_int, ct.c_int, _D, ct.POINTER(EcpgbInfo)]
+    L.ecpgb_job_create.argtypes = [P, ct.c_int]
+    L.ecpgb_job_create.restype = ct.c_void_p
+    L.ecpgb_job_run.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, _F, _F]
+    L.ecpgb_job_matrix.argtypes = [ct.c_void_p, ct.c_int, _D]
+    L.ecpgb_job_units.argtypes = [ct.c_void_p, _LL]
+    L.ecpgb_job_units.restype = ct.c_longlong
+    L.ecpgb_job_kernel_launches.argtypes = [ct.c_void_p]
+    L.ecpgb_job_free.argtypes = [ct.c_void_p]
+    L.ecpgb_job_free.restype = None
+    L.ecpgb_measure_peaks.argtypes = [_D]
+    L.ecpgb_last_error.restype = ct.c_char_p
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().ecpgb_last_error().decode()
+
+
+def _ptrs(s: EcpSystem):
+    d = lambda a: a.ctypes.data_as(_D)  # noqa: E731
+    i = lambda a: a.ctypes.data_as(_I)  # noqa: E731
+    return [s.n_atoms, d(s.geometry), i(s.shellsECP), i(s.KECP), i(s.lECP), d(s.nECP), d(s.dECP),
+            d(s.aECP), i(s.shellsBS), i(s.lBS), i(s.KBS), d(s.dBS), d(s.aBS),
+            int(s.largeGridOrder), float(s.tolerance), float(s.accuracy)]
+
+
+def c_system(s: EcpSystem) -> EcpgbSystem:
+    p = _ptrs(s)
+    return EcpgbSystem(p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[10], p[11],
+                       p[12], p[13], p[14], p[15])
+
+
+def get_integrals(s: EcpSystem, I: np.ndarray | None = None) -> np.ndarray:
+    """libECP's one-call interface: accumulates the upper triangle into I."""
+    if I is None:
+        I = np.zeros((s.dim, s.dim))
+    rc = lib().getIntegrals(*_ptrs(s), I.shape[1], I.ctypes.data_as(_D))
+    if rc != 0:
+        raise RuntimeError(f"getIntegrals failed: {last_error()}")
+    return I
+
+
+def get_integrals_info(s: EcpSystem, mode: int = ECPGB_FP64):
+    """(rc, matrix, info) through ecpgb_getIntegrals."""
+    I = np.zeros((s.dim, s.dim))
+    info = EcpgbInfo()
+    cs = c_system(s)
+    rc = lib().ecpgb_getIntegrals(ct.byref(cs), mode, s.dim, I.ctypes.data_as(_D), ct.byref(info))
+    if rc == 1:
+        raise RuntimeError(f"ecpgb_getIntegrals failed: {last_error()}")
+    return rc, I, info.as_dict()
+
+
+def blocks(s: EcpSystem, mode: int = ECPGB_FP64, with_status: bool = False):
+    """All emitted blocks in the reference's callback order.
+
+    Returns (meta, data) like the oracle: meta rows (A, s1, la, B, s2, lb, C,
+    type), data the blocks back to back.
+    """
+    L = lib()
+    cs = c_system(s)
+    nu, nv = ct.c_longlong(0), ct.c_longlong(0)
+    if L.ecpgb_layout(ct.byref(cs), ct.byref(nu), ct.byref(nv)):
+        raise RuntimeError(last_error())
+    vals = np.zeros(max(nv.value, 1))
+    offs = np.zeros(max(nu.value, 1), dtype=np.int64)
+    st = np.zeros(max(nu.value, 1), dtype=np.int32)
+    info = EcpgbInfo()
+    rc = L.ecpgb_blocks(ct.byref(cs), mode, vals.ctypes.data_as(_D), offs.ctypes.data_as(_LL),
+                        st.ctypes.data_as(_I), ct.byref(info))
+    if rc:
+        raise RuntimeError(f"ecpgb_blocks failed: {last_error()}")
+    meta, data = [], []
+    units = unit_table(s)
+    for u in range(nu.value):
+        if st[u] == UNIT_SKIPPED:
+            continue
+        A, s1, la, B, s2, lb, C = units[u]
+        n = ncart(la) * ncart(lb)
+        o = int(offs[u])
+        if st[u] == UNIT_FAIL_TYPE1:
+            break
+        meta.append((A, s1, la, B, s2, lb, C, 1))
+        data.append(vals[o:o + n])
+        if st[u] == UNIT_FAIL_TYPE2:
+            break
+        meta.append((A, s1, la, B, s2, lb, C, 2))
+        data.append(vals[o + n:o + 2 * n])
+    meta = np.array(meta, dtype=np.int32).reshape(-1, 8)
+    data = np.concatenate(data) if data else np.zeros(0)
+    if with_status:
+        return meta, data, st[:nu.value], info.as_dict()
+    return meta, data
+
+
+def unit_table(s: EcpSystem):
+    """(A, s1, la, B, s2, lb, C) per unit u = centre_rank * nPairs + pair."""
+    shells = []
+    for a in range(s.n_atoms):
+        for j in range(int(s.shellsBS[a])):
+            shells.append((a, j))
+    starts = np.concatenate([[0], np.cumsum(s.shellsBS)]).astype(int)
+    pairs = []
+    for A in range(s.n_atoms):
+        for B in range(A, s.n_atoms):
+            for i in range(int(s.shellsBS[A])):
+                for j in range(int(s.shellsBS[B])):
+                    if A == B and j < i:
+                        continue
+                    sa, sb = starts[A] + i, starts[B] + j
+                    pairs.append((A, i, int(s.lBS[sa]), B, j, int(s.lBS[sb])))
+    centres = [a for a in range(s.n_atoms) if s.shellsECP[a] > 0]
+    return [p + (C,) for C in centres for p in pairs]
+
+
+def calculate_blocks_via_callback(s: EcpSystem):
+    """Drives libECP_init / calculateECPIntegrals / libECP_free and records the
+    callback stream: (status, meta, data) in callback order."""
+    L = lib()
+    p = _ptrs(s)
+    # libECP_init reads (shellsECP, lECP, KECP) -- the definition's order
+    h = L.libECP_init(p[0], p[1], p[2], p[4], p[3], p[5], p[6], p[7], p[8], p[9], p[10], p[11],
+                      p[12], 0, -1, None, p[13], p[14], p[15])
+    if not h:
+        raise RuntimeError(f"libECP_init failed: {last_error()}")
+    meta, data = [], []
+    last = {"key": None, "type": 0}
+
+    def cb(A, sa, la, shifta, B, sb, lb, shiftb, C, I, _p):
+        key = (A, sa, B, sb, C)
+        t = 2 if (last["key"] == key and last["type"] == 1) else 1
+        last["key"], last["type"] = key, t
+        n = ncart(la) * ncart(lb)
+        meta.append((A, sa, la, B, sb, lb, C, t))
+        data.append(np.ctypeslib.as_array(I, shape=(n,)).copy())
+
+    c_cb = ECP_CALLBACK(cb)
+    try:
+        rc = L.calculateECPIntegrals(h, c_cb, None)
+    finally:
+        L.libECP_free(h)
+    meta = np.array(meta, dtype=np.int32).reshape(-1, 8)
+    return rc, meta, (np.concatenate(data) if data else np.zeros(0))
+
+
+class Job:
+    """Device-resident job: inputs copied to HBM once, then re-run."""
+
+    def __init__(self, s: EcpSystem, mode: int = ECPGB_FP64):
+        self.system = s
+        self._cs = c_system(s)
+        self._h = lib().ecpgb_job_create(ct.byref(self._cs), mode)
+        if not self._h:
+            raise RuntimeError(f"ecpgb_job_create failed: {last_error()}")
+
+    def run(self, n: int = 1, flush_l2: bool = True):
+        ms = np.zeros(n, dtype=np.float32)
+        mu = np.zeros(n, dtype=np.float32)
+        if lib().ecpgb_job_run(self._h, n, int(flush_l2), ms.ctypes.data_as(_F),
+                               mu.ctypes.data_as(_F)):
+            raise RuntimeError(f"ecpgb_job_run failed: {last_error()}")
+        return ms, mu
+
+    def matrix(self) -> np.ndarray:
+        I = np.zeros((self.system.dim, self.system.dim))
+        if lib().ecpgb_job_matrix(self._h, self.system.dim, I.ctypes.data_as(_D)):
+            raise RuntimeError(last_error())
+        return I
+
+    def units(self):
+        em = ct.c_longlong(0)
+        n = lib().ecpgb_job_units(self._h, ct.byref(em))
+        return n, em.value
+
+    def launches_per_run(self) -> int:
+        return lib().ecpgb_job_kernel_launches(self._h)
+
+    def close(self):
+        if self._h:
+            lib().ecpgb_job_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def measure_peaks() -> dict:
+    out = np.zeros(4)
+    if lib().ecpgb_measure_peaks(out.ctypes.data_as(_D)):
+        raise RuntimeError(last_error())
+    return {"fp64_fma_tflops": out[0], "fp32_fma_tflops": out[1], "mufu_ex2_gops": out[2],
+            "fp64_exp_gops": out[3]}

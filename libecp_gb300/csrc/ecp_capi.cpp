@@ -1,0 +1,220 @@
+// ecp_capi.cpp -- the C ABI of libecp_gb300.so.
+//
+// Drop-in symbols with chrr/libECP's prototypes and semantics:
+//   getIntegrals                       src/getIntegrals.h:7-13
+//   libECP_init / calculateECPIntegrals / libECP_free   src/libecp.h:15-29
+//   newECP / checkECP / getECP / evalECP / ECP_free      src/ecp.h:24-39
+// plus the ecpgb_* entry points of libecp_gb300.h.  Every integral is
+// computed by the CUDA kernels; without a GPU the calls fail with an error
+// (there is no CPU path).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "ecp.h"
+#include "ecp_host.h"
+#include "ecp_tables.h"
+#include "getIntegrals.h"
+#include "libecp.h"
+#include "libecp_gb300.h"
+
+using ecpgb::ncart;
+
+struct _libECPHandle {
+  ecpgb_system sys;
+  std::vector<int> shellsECP, KECP, lECP;  // ECP arrays are copied, as the reference copies its ECPs
+  std::vector<double> nECP, dECP, aECP;
+};
+
+struct ecpgb_job {
+  void *impl;
+};
+
+extern "C" {
+
+int getIntegrals(int nrAtoms, double *geometry, int *shellsECP, int *KECP, int *lECP, double *nECP,
+                 double *dECP, double *aECP, int *shellsBS, int *lBS, int *KBS, double *dBS,
+                 double *aBS, int largeGridOrder, double tolerance, double accuracy, int rowdim,
+                 double *I) {
+  ecpgb_system s = {nrAtoms, geometry, shellsECP, KECP, lECP, nECP, dECP, aECP,
+                    shellsBS, lBS, KBS, dBS, aBS, largeGridOrder, tolerance, accuracy};
+  int rc = ecpgb::run_matrix(s, ECPGB_FP64, rowdim, I, nullptr);
+  if (rc == 1 || rc < 0) {
+    printf("error initializing libECP\n");
+    fprintf(stderr, "libecp_gb300: %s\n", ecpgb::last_error());
+    return 1;
+  }
+  return 0;  // like the reference, quadrature failures are not reported here
+}
+
+libECPHandle *libECP_init(int nrAtoms, double *geometry, int *shellsECP, int *lECP, int *KECP,
+                          double *nECP, double *dECP, double *aECP, int *shellsBS, int *lBS,
+                          int *KBS, double *dBS, double *aBS, int n, int lmax, int *shellOrdering,
+                          int largeGridOrder, double tolerance, double accuracy) {
+  (void)lmax;
+  if (n != 0) {
+    ecpgb::set_error("derivative order %d: only n = 0 is implemented", n);
+    return nullptr;
+  }
+  if (shellOrdering != nullptr) {
+    ecpgb::set_error("custom Cartesian orderings are not implemented (pass NULL)");
+    return nullptr;
+  }
+  if (nrAtoms < 1) return nullptr;
+  auto *h = new _libECPHandle();
+  int nsh = 0, nt = 0;
+  h->shellsECP.assign(shellsECP, shellsECP + nrAtoms);
+  for (int i = 0; i < nrAtoms; i++) nsh += shellsECP[i] > 0 ? shellsECP[i] : 0;
+  h->lECP.assign(lECP, lECP + nsh);
+  h->KECP.assign(KECP, KECP + nsh);
+  for (int j = 0; j < nsh; j++) nt += KECP[j];
+  h->nECP.assign(nECP, nECP + nt);
+  h->dECP.assign(dECP, dECP + nt);
+  h->aECP.assign(aECP, aECP + nt);
+  h->sys = {nrAtoms, geometry, h->shellsECP.data(), h->KECP.data(), h->lECP.data(), h->nECP.data(),
+            h->dECP.data(), h->aECP.data(), shellsBS, lBS, KBS, dBS, aBS, largeGridOrder,
+            tolerance, accuracy};
+  ecpgb::Parsed P;
+  if (ecpgb::parse_system(h->sys, P)) {
+    delete h;
+    return nullptr;
+  }
+  ecpgb::HostTables t;
+  ecpgb::build_tables({P.maxLECP, P.maxLBS, largeGridOrder, tolerance, accuracy}, t);
+  if (t.status) {  // e.g. the Bessel series does not converge (src/libecp.c:181-185)
+    delete h;
+    return nullptr;
+  }
+  return h;
+}
+
+int calculateECPIntegrals(libECPHandle *h, ECPCallback cb, void *args) {
+  long long nUnits = 0, nValues = 0;
+  if (!h || ecpgb::layout(h->sys, &nUnits, &nValues)) return -1;
+  std::vector<double> values(nValues > 0 ? nValues : 1);
+  std::vector<long long> offsets(nUnits > 0 ? nUnits : 1);
+  std::vector<int> status(nUnits > 0 ? nUnits : 1);
+  ecpgb_info info;
+  ecpgb::Parsed P;
+  if (ecpgb::run_blocks(h->sys, ECPGB_FP64, values.data(), offsets.data(), status.data(), &info, &P)) {
+    fprintf(stderr, "libecp_gb300: %s\n", ecpgb::last_error());
+    return -1;
+  }
+  std::vector<double> blk;
+  for (long long u = 0; u < nUnits; u++) {
+    int st = status[u];
+    if (st == ECPGB_UNIT_SKIPPED) continue;
+    int c = (int)(u / P.nPairs), p = (int)(u % P.nPairs);
+    int sa = P.pairA[p], sb = P.pairB[p], la = P.shL[sa], lb = P.shL[sb];
+    int A = P.shAtom[sa], B = P.shAtom[sb], C = P.ctrAtom[c];
+    size_t nb = (size_t)ncart(la) * ncart(lb);
+    const double *b1 = values.data() + offsets[u];
+    if (st == ECPGB_UNIT_FAIL_TYPE1) return 1;
+    blk.assign(b1, b1 + nb);
+    cb(A, P.shLocal[sa], la, 0, B, P.shLocal[sb], lb, 0, C, blk.data(), args);
+    if (st == ECPGB_UNIT_FAIL_TYPE2) return 2;
+    blk.assign(b1 + nb, b1 + 2 * nb);
+    cb(A, P.shLocal[sa], la, 0, B, P.shLocal[sb], lb, 0, C, blk.data(), args);
+  }
+  return 0;
+}
+
+void libECP_free(libECPHandle *h) { delete h; }
+
+// ------------------------------------------------------------ ECP helpers
+
+ECP *newECP(const int L, const int N) {
+  ECP *U = (ECP *)malloc(sizeof(ECP));
+  U->L = L;
+  U->N = N;
+  U->U_l = (ECPGauss *)calloc(N > 0 ? N : 1, sizeof(ECPGauss));
+  for (int i = 0; i < N; i++) U->U_l[i].l = -1;
+  return U;
+}
+
+int checkECP(const ECP *U) {
+  int l = 0;
+  for (int i = 0; i < U->N; i++) {
+    const ECPGauss *g = &U->U_l[i];
+    if (l > g->l || U->L < g->l) return 1;
+    if (l < g->l) l = g->l;
+  }
+  return 0;
+}
+
+int getECP(const ECP *U, const int l, ECPGauss **U_l) {
+  int n = 0;
+  for (int i = 0; i < U->N; i++) n += U->U_l[i].l == l;
+  *U_l = (ECPGauss *)malloc(sizeof(ECPGauss) * (n > 0 ? n : 1));
+  for (int i = 0, k = 0; i < U->N; i++)
+    if (U->U_l[i].l == l) (*U_l)[k++] = U->U_l[i];
+  return n;
+}
+
+double evalECP(const ECP *U, const int l, const double r) {
+  double pot = 0.0, r2 = r * r;
+  for (int i = 0; i < U->N; i++) {
+    const ECPGauss *g = &U->U_l[i];
+    if (g->l == l) pot += pow(r, g->n) * g->d * exp(-g->a * r2);
+  }
+  return pot;
+}
+
+void ECP_free(ECP *E) {
+  if (!E) return;
+  free(E->U_l);
+  free(E);
+}
+
+// ------------------------------------------------------------ ecpgb_*
+
+int ecpgb_layout(const ecpgb_system *s, long long *nUnits, long long *nValues) {
+  return s ? ecpgb::layout(*s, nUnits, nValues) : 1;
+}
+
+int ecpgb_blocks(const ecpgb_system *s, int mode, double *values, long long *offsets, int *status,
+                 ecpgb_info *info) {
+  if (!s) return 1;
+  return ecpgb::run_blocks(*s, mode, values, offsets, status, info, nullptr) ? 1 : 0;
+}
+
+int ecpgb_getIntegrals(const ecpgb_system *s, int mode, int rowdim, double *I, ecpgb_info *info) {
+  if (!s) return 1;
+  int rc = ecpgb::run_matrix(*s, mode, rowdim, I, info);
+  return rc < 0 ? 1 : rc;
+}
+
+ecpgb_job *ecpgb_job_create(const ecpgb_system *s, int mode) {
+  if (!s) return nullptr;
+  void *impl = ecpgb::job_create(*s, mode);
+  if (!impl) return nullptr;
+  return new ecpgb_job{impl};
+}
+
+int ecpgb_job_run(ecpgb_job *j, int nRuns, int flushL2, float *msRun, float *msUnit) {
+  return j ? ecpgb::job_run(j->impl, nRuns, flushL2, msRun, msUnit) : 1;
+}
+
+int ecpgb_job_matrix(ecpgb_job *j, int rowdim, double *I) {
+  return j ? ecpgb::job_matrix(j->impl, rowdim, I) : 1;
+}
+
+long long ecpgb_job_units(const ecpgb_job *j, long long *emitted) {
+  return j ? ecpgb::job_units(j->impl, emitted) : 0;
+}
+
+int ecpgb_job_kernel_launches(const ecpgb_job *j) { return j ? ecpgb::job_launches(j->impl) : 0; }
+
+void ecpgb_job_free(ecpgb_job *j) {
+  if (!j) return;
+  ecpgb::job_free(j->impl);
+  delete j;
+}
+
+int ecpgb_measure_peaks(double *out) { return ecpgb::measure_peaks(out); }
+
+const char *ecpgb_last_error(void) { return ecpgb::last_error(); }
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+// ecp_engine.h -- device-side job description shared by the host driver
+// (ecp_engine.cu) and the kernels (ecp_fp64.cu).
+//
+// HBM layout of one job (all arrays device-resident, FP64 unless noted):
+//   inputs      geometry[3*nAtoms]; per shell l, K, first primitive, atom,
+//               AO offset; per primitive exponent/coefficient; per ECP centre
+//               atom, L, term range; per term l, n, d, a; the pair list in the
+//               reference's loop order (A, B>=A, s1, s2).
+//   per centre  r^k U_l on the small grid, point-major [383][maxLECP][nk];
+//               the local channel U_L [383]; the screened grid end.
+//   per centre  rAC, dAC, unit-sphere polynomials and the contracted angular
+//   and atom    table [lambda][lm][Cartesian] of src/angular_integrals.c:105.
+//   per centre  screening window (start, end, skip) and the F table,
+//   and shell   point-major [383][nF], zero outside the window.
+//   output      per (centre, pair) unit a type-1 block then a type-2 block,
+//               NCART(la) x NCART(lb) each, row-major; a status word per unit;
+//               the upper triangle of the AO matrix.
+// Units are numbered u = centre * nPairs + pair, i.e. the reference's
+// callback order (src/libecp.c:256-397).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace ecpgb {
+
+constexpr int kSmallOrder = 383;       // PS93(128) abscissae
+constexpr int kMaxLargeOrder = 4095;   // PSM92 abscissae (largeGridOrder < 8192)
+constexpr int kMaxContraction = 16;    // primitives per shell
+constexpr int kUnitThreads = 128;      // threads per unit CTA
+constexpr int kChunkPairs = 64;        // (lower, upper) pairs per fallback chunk
+constexpr int kMaxWalkers = 512;       // large-grid quadratures integrated per pass
+
+// Unit status words.
+enum : int {
+  kUnitDone = 0,        // both blocks written
+  kUnitSkipped = 1,     // screened out: the reference makes no callback
+  kUnitFailType1 = 2,   // a type-1 large-grid quadrature did not converge
+  kUnitFailType2 = 3,   // a type-2 large-grid quadrature did not converge
+  kUnitBadInput = 4,    // sizes beyond what the kernels are compiled for
+};
+
+struct DevJob {
+  // sizes
+  int nAtoms, nShells, nPrims, nCentres, nPairs, dim;
+  int maxLECP, maxLBS, maxLambda, nk, nF, tmDim, tabL, besselN;
+  int omD1, omD2;              // omega dims [nsph(maxLECP)][omD1][omD2]
+  int angLam, angLM, angC;     // per (centre, atom) angular table dims
+  int uspD;                    // unit-sphere polynomial table side (maxLBS + 1)
+  int largeOrder;
+  double tol, acc, lnAcc1, lnAcc2;
+  // inputs
+  const double *geom;
+  const int *shL, *shK, *shP, *shAtom, *shAO;
+  const double *primA, *primD;
+  const int *ctrAtom, *ctrL, *ctrT0, *ctrNT;
+  const int *termL;
+  const double *termN, *termD, *termA;
+  const int *pairA, *pairB;
+  const long long *pairOff;    // value offset of the pair's two blocks within a centre
+  long long centreStride;      // values per centre
+  // used-triple lists of the type-2 angular linking, per (la, lb, l)
+  const int *itemOff, *itemCnt, *items;
+  // tables
+  const double *xSmall, *wSmall, *xLarge, *wLarge;
+  const double *besT, *besC;
+  const double *p2s, *fac, *dfac;
+  const int *atomMaxL;
+  const int *ijk, *ijkIdx;
+  const double *omega;
+  // per-job work arrays
+  double *radius;
+  double *utab, *uL;
+  int *gridEnd;
+  int *win;
+  double *F;
+  double *cgeo, *usp, *ang;
+  double *out;
+  int *status;
+  double *mat;
+  int *errWord;          // [0] first failing unit (atomicMin), [1] input error flags
+};
+
+// Shared-memory layout of the unit kernel (offsets in doubles).
+struct UnitSmem {
+  int K1, R1, EX1, U1, rsh, Q, chi, J, Fa, Fb, T, st, ck, total;
+  int qItems;     // per-thread walker state capacity (items)
+  int ckStride;   // doubles per chunk point
+};
+
+__host__ __device__ inline UnitSmem unit_smem_layout(int LB, int LE, int nF) {
+  UnitSmem s{};
+  int LAB = 2 * LB, nA = LAB + 1, nE = LE > 0 ? LE : 1;
+  int nc = (LB + 1) * (LB + 2) * (LB + 3) / 6, nct = (LB + 1) * (LB + 2) / 2;
+  int o = 0;
+  s.chi = o; o += nc * nc;
+  s.J = o; o += nct * nc;
+  s.rsh = o; o += nA * nA;
+  s.Q = o; o += nA * nA;
+  int base = o;
+  // type-1 phase
+  s.K1 = o; o += kSmallOrder * nA;
+  s.R1 = o; o += kSmallOrder * nA;
+  s.EX1 = o; o += kSmallOrder;
+  s.U1 = o; o += kSmallOrder;
+  int t1end = o;
+  // type-2 phase (overlays the type-1 tables)
+  o = base;
+  s.Fa = o; o += kSmallOrder * nF;
+  s.Fb = o; o += kSmallOrder * nF;
+  s.T = o; o += nE * (LB + nE) * (LB + nE) * nA;
+  int t2end = o;
+  o = t1end > t2end ? t1end : t2end;
+  // walker state for large-grid items (I, p, q, result) and chunk tables;
+  // failed items beyond kMaxWalkers are integrated in further passes
+  s.qItems = kMaxWalkers;
+  if (s.qItems < nA * nA) s.qItems = nA * nA;
+  s.st = o; o += 4 * s.qItems;
+  // chunk point: w, ex, visited, then type-2 U[l], r^k, Ka, Kb or type-1 U, r^k, K
+  s.ckStride = 3 + nE + nA + 2 * (LB + nE);
+  if (s.ckStride < 4 + 2 * nA) s.ckStride = 4 + 2 * nA;
+  s.ck = o; o += (2 * kChunkPairs + 1) * s.ckStride;
+  s.total = o;
+  return s;
+}
+
+// Host-side launchers (ecp_fp64.cu).
+int upload_schedules(const int *s93slot, int s93n, const int *s93lvEnd, const int *s93lvJ,
+                     const int *s93lvN, int s93levels, const int *s92slot, int s92n,
+                     const int *s92lvEnd, const int *s92lvN, int s92levels, void *stream);
+// Launches the six-kernel pipeline on `stream`; u0/u1 (may be null) are
+// recorded around the per-unit kernel.
+int launch_fp64_pipeline(const DevJob &job, cudaStream_t stream, size_t smemBytes, cudaEvent_t u0,
+                         cudaEvent_t u1);
+
+}  // namespace ecpgb

@@ -1,0 +1,544 @@
+// ecp_host.cu -- host side of the engine: parsing, resident tables, device
+// buffers, the run sequence, the device-resident job and the pipe probe.
+//
+// One run of a job on the engine's stream:
+//   one H2D copy of all inputs (packed into a pinned staging buffer), memsets
+//   of the AO matrix / block buffer / error words, the six-kernel FP64
+//   pipeline, one D2H copy of the result (matrix or blocks) and the error
+//   words.  Tables (grids, Bessel table, angular table, ...) are built once
+//   per key on the host and stay resident on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ecp_engine.h"
+#include "ecp_host.h"
+#include "ecp_tables.h"
+
+namespace ecpgb {
+
+static thread_local std::string g_err;
+const char *last_error() { return g_err.c_str(); }
+void set_error(const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+
+#define CUDA_OK(x)                                                                   \
+  do {                                                                               \
+    cudaError_t e_ = (x);                                                            \
+    if (e_ != cudaSuccess) {                                                         \
+      set_error("CUDA error %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return -1;                                                                     \
+    }                                                                                \
+  } while (0)
+
+// ------------------------------------------------------------------ parsing
+
+int parse_system(const ecpgb_system &s, Parsed &P) {
+  P = Parsed();
+  if (s.nrAtoms < 1 || !s.geometry || !s.shellsECP || !s.shellsBS) {
+    set_error("invalid system: nrAtoms < 1 or missing arrays");
+    return 1;
+  }
+  P.nAtoms = s.nrAtoms;
+  P.geom.assign(s.geometry, s.geometry + 3 * s.nrAtoms);
+  P.atomMaxL.assign(s.nrAtoms, 0);
+  P.atomShell0.assign(s.nrAtoms, 0);
+  int sh = 0, prim = 0, ao = 0;
+  for (int a = 0; a < s.nrAtoms; a++) {
+    P.atomShell0[a] = sh;
+    if (s.shellsBS[a] < 0) { set_error("negative shell count on atom %d", a); return 1; }
+    for (int j = 0; j < s.shellsBS[a]; j++, sh++) {
+      int l = s.lBS[sh], k = s.KBS[sh];
+      if (l < 0 || l > kMaxLBasis) { set_error("basis l=%d outside 0..%d", l, kMaxLBasis); return 1; }
+      if (k < 1 || k > kMaxContraction) {
+        set_error("contraction %d outside 1..%d", k, kMaxContraction);
+        return 1;
+      }
+      P.shL.push_back(l); P.shK.push_back(k); P.shP.push_back(prim); P.shAtom.push_back(a);
+      P.shAO.push_back(ao); P.shLocal.push_back(j);
+      for (int p = 0; p < k; p++) { P.primA.push_back(s.aBS[prim + p]); P.primD.push_back(s.dBS[prim + p]); }
+      prim += k;
+      ao += ncart(l);
+      P.atomMaxL[a] = std::max(P.atomMaxL[a], l);
+      P.maxLBS = std::max(P.maxLBS, l);
+    }
+  }
+  P.nShells = sh;
+  P.nPrims = prim;
+  P.dim = ao;
+  // ECPs (src/libecp.c:93-127): per atom its shells' terms in order
+  int esh = 0, term = 0;
+  for (int a = 0; a < s.nrAtoms; a++) {
+    if (s.shellsECP[a] <= 0) {
+      esh += 0;
+      continue;
+    }
+    int L = 0, t0 = (int)P.termL.size();
+    for (int j = 0; j < s.shellsECP[a]; j++, esh++) {
+      int l = s.lECP[esh], k = s.KECP[esh];
+      if (l < 0 || l > kMaxLEcp || k < 0) {
+        set_error("ECP shell with l=%d (0..%d) or K=%d", l, kMaxLEcp, k);
+        return 1;
+      }
+      L = std::max(L, l);
+      for (int t = 0; t < k; t++, term++) {
+        P.termL.push_back(l);
+        P.termN.push_back(s.nECP[term]);
+        P.termD.push_back(s.dECP[term]);
+        P.termA.push_back(s.aECP[term]);
+      }
+    }
+    P.ctrAtom.push_back(a);
+    P.ctrL.push_back(L);
+    P.ctrT0.push_back(t0);
+    P.ctrNT.push_back((int)P.termL.size() - t0);
+    P.maxLECP = std::max(P.maxLECP, L);
+  }
+  P.nCentres = (int)P.ctrAtom.size();
+  // shell pairs in the reference's loop order (src/libecp.c:278-312)
+  long long off = 0;
+  for (int A = 0; A < s.nrAtoms; A++)
+    for (int B = A; B < s.nrAtoms; B++)
+      for (int i = 0; i < s.shellsBS[A]; i++)
+        for (int j = 0; j < s.shellsBS[B]; j++) {
+          if (A == B && j < i) continue;
+          int sa = P.atomShell0[A] + i, sb = P.atomShell0[B] + j;
+          P.pairA.push_back(sa);
+          P.pairB.push_back(sb);
+          P.pairOff.push_back(off);
+          off += 2LL * ncart(P.shL[sa]) * ncart(P.shL[sb]);
+        }
+  P.nPairs = (int)P.pairA.size();
+  P.centreStride = off;
+  P.largeGridOrder = s.largeGridOrder;
+  P.tol = s.tolerance;
+  P.acc = s.accuracy;
+  if (s.largeGridOrder < 384 || s.largeGridOrder >= 2 * (kMaxLargeOrder + 1)) {
+    set_error("largeGridOrder %d outside 384..%d", s.largeGridOrder, 2 * (kMaxLargeOrder + 1) - 1);
+    return 1;
+  }
+  if (!(s.accuracy > 0) || !(s.tolerance > 0)) {
+    set_error("tolerance and accuracy must be positive");
+    return 1;
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------ device tables
+
+struct DevTables {
+  TableKey key{};
+  HostTables host;
+  DBuf<double> xs, ws, xl, wl, besT, besC, p2s, fac, dfac, omega;
+  DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items;
+  int nItemsMax = 0;
+};
+
+struct Engine {
+  std::mutex mu;
+  cudaStream_t stream = nullptr;
+  std::vector<std::unique_ptr<DevTables>> tables;
+  const DevTables *schedOwner = nullptr;
+  JobBuffers shared;
+  DBuf<char> flush;
+  bool init = false;
+
+  int ensure_init() {
+    if (init) return 0;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) {
+      set_error("no CUDA device: the ECP engine runs on the GPU only");
+      return -1;
+    }
+    CUDA_OK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    init = true;
+    return 0;
+  }
+
+  const DevTables *get_tables(const TableKey &key) {
+    for (auto &t : tables)
+      if (t->key == key) return t.get();
+    auto t = std::make_unique<DevTables>();
+    t->key = key;
+    build_tables(key, t->host);
+    if (t->host.status) {
+      set_error(t->host.status == 1 ? "Bessel series did not converge" : "table sizes out of range");
+      return nullptr;
+    }
+    HostTables &h = t->host;
+    bool ok = t->xs.upload(h.xs, stream) && t->ws.upload(h.ws, stream) && t->xl.upload(h.xl, stream) &&
+              t->wl.upload(h.wl, stream) && t->besT.upload(h.besselT, stream) &&
+              t->besC.upload(h.besselC, stream) && t->p2s.upload(h.poly2sph, stream) &&
+              t->fac.upload(h.fac, stream) && t->dfac.upload(h.dfac, stream) &&
+              t->omega.upload(h.omega, stream) && t->ijk.upload(h.ijk, stream) &&
+              t->ijkIdx.upload(h.ijkIndex, stream);
+    // used-triple lists per (la, lb, l)
+    int LB = h.maxLBS, LE = h.maxLECP > 0 ? h.maxLECP : 1;
+    std::vector<int> off, cnt, items, tmp;
+    for (int la = 0; la <= LB; la++)
+      for (int lb = 0; lb <= LB; lb++) {
+        int tot = 0;
+        for (int l = 0; l < LE; l++) {
+          used_triples(la, lb, l, tmp);
+          off.push_back((int)items.size());
+          cnt.push_back((int)tmp.size());
+          items.insert(items.end(), tmp.begin(), tmp.end());
+          tot += (int)tmp.size();
+        }
+        t->nItemsMax = std::max(t->nItemsMax, tot);
+      }
+    ok = ok && t->itemOff.upload(off, stream) && t->itemCnt.upload(cnt, stream) &&
+         t->items.upload(items, stream);
+    if (!ok) {
+      set_error("device allocation failed for tables");
+      return nullptr;
+    }
+    if (t->nItemsMax > 2048) {
+      set_error("angular momenta too high for the FP64 kernel (%d radial items)", t->nItemsMax);
+      return nullptr;
+    }
+    if (tables.size() >= 8) tables.erase(tables.begin());
+    tables.push_back(std::move(t));
+    return tables.back().get();
+  }
+
+  int use_schedules(const DevTables *t) {
+    if (schedOwner == t) return 0;
+    const HostTables &h = t->host;
+    int rc = upload_schedules(h.s93.slot.data(), (int)h.s93.slot.size(), h.s93.lvEnd.data(),
+                              h.s93.lvJ.data(), h.s93.lvN.data(), h.s93.nLevels, h.s92.slot.data(),
+                              (int)h.s92.slot.size(), h.s92.lvEnd.data(), h.s92.lvN.data(),
+                              h.s92.nLevels, stream);
+    if (rc) {
+      set_error("schedule upload failed (%d)", rc);
+      return -1;
+    }
+    schedOwner = t;
+    return 0;
+  }
+};
+
+static Engine &engine() {
+  static Engine *e = new Engine();  // lives until exit; device memory is released by the driver
+  return *e;
+}
+
+// ------------------------------------------------------------ job set-up
+
+static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Packs the inputs into the pinned staging buffer, copies them to the device
+// and fills the DevJob's input and work pointers.
+static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J) {
+  const HostTables &h = T->host;
+  std::memset(&J, 0, sizeof J);
+  J.nAtoms = P.nAtoms; J.nShells = P.nShells; J.nPrims = P.nPrims; J.nCentres = P.nCentres;
+  J.nPairs = P.nPairs; J.dim = P.dim;
+  J.maxLECP = h.maxLECP; J.maxLBS = h.maxLBS; J.maxLambda = h.maxLambda; J.nk = h.nk; J.nF = h.nF;
+  J.tmDim = h.tmDim; J.tabL = h.tabL; J.besselN = h.besselN; J.omD1 = h.omD1; J.omD2 = h.omD2;
+  int LE = h.maxLECP > 0 ? h.maxLECP : 1;
+  J.angLam = h.maxLECP + h.maxLBS + 1;
+  J.angLM = LE * LE;
+  J.angC = ncum(h.maxLBS);
+  J.uspD = h.maxLBS + 1;
+  J.largeOrder = (int)h.xl.size();
+  J.tol = P.tol; J.acc = P.acc;
+  J.lnAcc1 = std::log(P.acc) - 2;
+  J.lnAcc2 = std::log(1.0E-14) - 2;
+  // --- inputs: one packed H2D copy
+  struct Piece { const void *src; size_t bytes; size_t off; };
+  std::vector<Piece> pcs;
+  size_t tot = 0;
+  auto add = [&](const void *src, size_t bytes) {
+    pcs.push_back({src, bytes, tot});
+    tot += al(bytes ? bytes : 1);
+    return pcs.size() - 1;
+  };
+  size_t iGeom = add(P.geom.data(), 8 * P.geom.size()), iPA = add(P.primA.data(), 8 * P.primA.size()),
+         iPD = add(P.primD.data(), 8 * P.primD.size()), iTN = add(P.termN.data(), 8 * P.termN.size()),
+         iTD = add(P.termD.data(), 8 * P.termD.size()), iTA = add(P.termA.data(), 8 * P.termA.size()),
+         iShL = add(P.shL.data(), 4 * P.shL.size()), iShK = add(P.shK.data(), 4 * P.shK.size()),
+         iShP = add(P.shP.data(), 4 * P.shP.size()), iShA = add(P.shAtom.data(), 4 * P.shAtom.size()),
+         iShO = add(P.shAO.data(), 4 * P.shAO.size()), iAM = add(P.atomMaxL.data(), 4 * P.atomMaxL.size()),
+         iCA = add(P.ctrAtom.data(), 4 * P.ctrAtom.size()), iCL = add(P.ctrL.data(), 4 * P.ctrL.size()),
+         iCT = add(P.ctrT0.data(), 4 * P.ctrT0.size()), iCN = add(P.ctrNT.data(), 4 * P.ctrNT.size()),
+         iTL = add(P.termL.data(), 4 * P.termL.size()), iPrA = add(P.pairA.data(), 4 * P.pairA.size()),
+         iPrB = add(P.pairB.data(), 4 * P.pairB.size()), iPO = add(P.pairOff.data(), 8 * P.pairOff.size());
+  if (!B.pinned.ensure(tot) || !B.in.ensure(tot)) {
+    set_error("allocation of %zu input bytes failed", tot);
+    return -1;
+  }
+  for (auto &p : pcs)
+    if (p.bytes) std::memcpy(B.pinned.p + p.off, p.src, p.bytes);
+  CUDA_OK(cudaMemcpyAsync(B.in.p, B.pinned.p, tot, cudaMemcpyHostToDevice, E.stream));
+  B.h2dBytes = (long long)tot;
+  auto dp = [&](size_t i) { return (void *)(B.in.p + pcs[i].off); };
+  J.geom = (const double *)dp(iGeom); J.primA = (const double *)dp(iPA); J.primD = (const double *)dp(iPD);
+  J.termN = (const double *)dp(iTN); J.termD = (const double *)dp(iTD); J.termA = (const double *)dp(iTA);
+  J.shL = (const int *)dp(iShL); J.shK = (const int *)dp(iShK); J.shP = (const int *)dp(iShP);
+  J.shAtom = (const int *)dp(iShA); J.shAO = (const int *)dp(iShO); J.atomMaxL = (const int *)dp(iAM);
+  J.ctrAtom = (const int *)dp(iCA); J.ctrL = (const int *)dp(iCL); J.ctrT0 = (const int *)dp(iCT);
+  J.ctrNT = (const int *)dp(iCN); J.termL = (const int *)dp(iTL); J.pairA = (const int *)dp(iPrA);
+  J.pairB = (const int *)dp(iPrB); J.pairOff = (const long long *)dp(iPO);
+  J.centreStride = P.centreStride;
+  // --- tables
+  J.itemOff = T->itemOff.p; J.itemCnt = T->itemCnt.p; J.items = T->items.p;
+  J.xSmall = T->xs.p; J.wSmall = T->ws.p; J.xLarge = T->xl.p; J.wLarge = T->wl.p;
+  J.besT = T->besT.p; J.besC = T->besC.p; J.p2s = T->p2s.p; J.fac = T->fac.p; J.dfac = T->dfac.p;
+  J.ijk = T->ijk.p; J.ijkIdx = T->ijkIdx.p; J.omega = T->omega.p;
+  // --- work arrays
+  const size_t nc = P.nCentres, ns = P.nShells, na = P.nAtoms, O = kSmallOrder;
+  bool ok = B.radius.ensure(ns + 1) && B.utab.ensure(nc * O * LE * h.nk + 1) && B.uL.ensure(nc * O + 1) &&
+            B.gridEnd.ensure(nc + 1) && B.win.ensure(nc * ns * 3 + 1) && B.F.ensure(nc * ns * O * h.nF + 1) &&
+            B.cgeo.ensure(nc * na * 4 + 1) && B.usp.ensure(nc * na * J.uspD * J.uspD * J.uspD + 1) &&
+            B.ang.ensure(nc * na * (size_t)J.angLam * J.angLM * J.angC + 1) &&
+            B.out.ensure(nc * (size_t)P.centreStride + 1) && B.status.ensure(nc * (size_t)P.nPairs + 1) &&
+            B.mat.ensure((size_t)P.dim * P.dim + 1) && B.err.ensure(2);
+  if (!ok) {
+    set_error("device allocation failed for the job's work arrays");
+    return -1;
+  }
+  J.radius = B.radius.p; J.utab = B.utab.p; J.uL = B.uL.p; J.gridEnd = B.gridEnd.p; J.win = B.win.p;
+  J.F = B.F.p; J.cgeo = B.cgeo.p; J.usp = B.usp.p; J.ang = B.ang.p; J.out = B.out.p;
+  J.status = B.status.p; J.mat = B.mat.p; J.errWord = B.err.p;
+  UnitSmem L = unit_smem_layout(h.maxLBS, h.maxLECP, h.nF);
+  B.smem = sizeof(double) * (size_t)L.total;
+  return 0;
+}
+
+// Resets the per-run outputs and launches the pipeline.
+static int run_pipeline(Engine &E, JobBuffers &B, const DevJob &J, cudaEvent_t u0, cudaEvent_t u1) {
+  int init[2] = {INT_MAX, 0};
+  std::memcpy(B.pinnedErr, init, sizeof init);
+  CUDA_OK(cudaMemcpyAsync(B.err.p, B.pinnedErr, sizeof init, cudaMemcpyHostToDevice, E.stream));
+  CUDA_OK(cudaMemsetAsync(B.mat.p, 0, sizeof(double) * (size_t)J.dim * J.dim, E.stream));
+  int rc = launch_fp64_pipeline(J, E.stream, B.smem, u0, u1);
+  if (rc) {
+    set_error("kernel launch failed (%d): %s", rc, cudaGetErrorString(cudaGetLastError()));
+    return -1;
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------ public runs
+
+int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_info *info) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  if (mode != ECPGB_FP64) { set_error("unknown mode %d", mode); return 1; }
+  if (E.ensure_init()) return 1;
+  Parsed P;
+  if (parse_system(s, P)) return 1;
+  if (rowdim < P.dim) { set_error("rowdim %d < basis dimension %d", rowdim, P.dim); return 1; }
+  if (P.nCentres == 0 || P.nPairs == 0) {
+    if (info) { std::memset(info, 0, sizeof *info); info->firstFailed = -1; }
+    return 0;
+  }
+  const DevTables *T = E.get_tables({P.maxLECP, P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
+  if (!T || E.use_schedules(T)) return 1;
+  JobBuffers &B = E.shared;
+  DevJob J;
+  if (stage_job(E, P, T, B, J)) return 1;
+  cudaEvent_t e0, e1, u0, u1;
+  cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
+  cudaEventRecord(e0, E.stream);
+  if (run_pipeline(E, B, J, u0, u1)) return 1;
+  cudaEventRecord(e1, E.stream);
+  size_t mb = sizeof(double) * (size_t)P.dim * P.dim;
+  if (!B.pinnedOut.ensure(mb)) { set_error("pinned allocation failed"); return 1; }
+  cudaMemcpyAsync(B.pinnedOut.p, B.mat.p, mb, cudaMemcpyDeviceToHost, E.stream);
+  cudaMemcpyAsync(B.pinnedErr, B.err.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, E.stream);
+  cudaError_t ce = cudaStreamSynchronize(E.stream);
+  if (ce != cudaSuccess) { set_error("device error: %s", cudaGetErrorString(ce)); return 1; }
+  float ms = 0, msu = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventElapsedTime(&msu, u0, u1);
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(u0); cudaEventDestroy(u1);
+  const double *M = (const double *)B.pinnedOut.p;
+  for (int i = 0; i < P.dim; i++)
+    for (int j = i; j < P.dim; j++) I[(size_t)i * rowdim + j] += M[(size_t)i * P.dim + j];
+  int err0 = B.pinnedErr[0], err1 = B.pinnedErr[1];
+  if (info) {
+    info->units = (long long)P.nCentres * P.nPairs;
+    info->emitted = -1;
+    info->firstFailed = err0 == INT_MAX ? -1 : err0;
+    info->values = (long long)P.nCentres * P.centreStride;
+    info->msGpu = ms;
+    info->msUnitKernel = msu;
+    info->h2dBytes = B.h2dBytes;
+    info->d2hBytes = (long long)mb + 8;
+  }
+  if (err1) { set_error("a shell radius did not converge (Newton, 40 steps)"); return 1; }
+  return err0 == INT_MAX ? 0 : 2;
+}
+
+int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offsets, int *status,
+               ecpgb_info *info, Parsed *parsedOut) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  if (mode != ECPGB_FP64) { set_error("unknown mode %d", mode); return 1; }
+  if (E.ensure_init()) return 1;
+  Parsed P;
+  if (parse_system(s, P)) return 1;
+  if (parsedOut) *parsedOut = P;
+  const long long nUnits = (long long)P.nCentres * P.nPairs;
+  if (nUnits == 0) {
+    if (info) { std::memset(info, 0, sizeof *info); info->firstFailed = -1; }
+    return 0;
+  }
+  const DevTables *T = E.get_tables({P.maxLECP, P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
+  if (!T || E.use_schedules(T)) return 1;
+  JobBuffers &B = E.shared;
+  DevJob J;
+  if (stage_job(E, P, T, B, J)) return 1;
+  const size_t nv = (size_t)P.nCentres * P.centreStride;
+  cudaMemsetAsync(B.out.p, 0, sizeof(double) * nv, E.stream);
+  cudaEvent_t e0, e1, u0, u1;
+  cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
+  cudaEventRecord(e0, E.stream);
+  if (run_pipeline(E, B, J, u0, u1)) return 1;
+  cudaEventRecord(e1, E.stream);
+  if (values) cudaMemcpyAsync(values, B.out.p, sizeof(double) * nv, cudaMemcpyDeviceToHost, E.stream);
+  std::vector<int> st(nUnits);
+  cudaMemcpyAsync(st.data(), B.status.p, sizeof(int) * nUnits, cudaMemcpyDeviceToHost, E.stream);
+  cudaMemcpyAsync(B.pinnedErr, B.err.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, E.stream);
+  cudaError_t ce = cudaStreamSynchronize(E.stream);
+  if (ce != cudaSuccess) { set_error("device error: %s", cudaGetErrorString(ce)); return 1; }
+  float ms = 0, msu = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventElapsedTime(&msu, u0, u1);
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(u0); cudaEventDestroy(u1);
+  long long emitted = 0;
+  for (long long u = 0; u < nUnits; u++) {
+    if (status) status[u] = st[u];
+    if (offsets) offsets[u] = (u / P.nPairs) * P.centreStride + P.pairOff[u % P.nPairs];
+    emitted += st[u] == kUnitDone;
+  }
+  int err0 = B.pinnedErr[0], err1 = B.pinnedErr[1];
+  if (info) {
+    info->units = nUnits;
+    info->emitted = emitted;
+    info->firstFailed = err0 == INT_MAX ? -1 : err0;
+    info->values = (long long)nv;
+    info->msGpu = ms;
+    info->msUnitKernel = msu;
+    info->h2dBytes = B.h2dBytes;
+    info->d2hBytes = (long long)(sizeof(double) * nv + sizeof(int) * nUnits);
+  }
+  if (err1) { set_error("a shell radius did not converge (Newton, 40 steps)"); return 1; }
+  return 0;
+}
+
+int layout(const ecpgb_system &s, long long *nUnits, long long *nValues) {
+  Parsed P;
+  if (parse_system(s, P)) return 1;
+  if (nUnits) *nUnits = (long long)P.nCentres * P.nPairs;
+  if (nValues) *nValues = (long long)P.nCentres * P.centreStride;
+  return 0;
+}
+
+// ------------------------------------------------------------ resident jobs
+
+struct ResidentJob {
+  Parsed P;
+  const DevTables *T = nullptr;
+  JobBuffers B;
+  DevJob J;
+  int launches = 6;
+};
+
+void *job_create(const ecpgb_system &s, int mode) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  if (mode != ECPGB_FP64) { set_error("unknown mode %d", mode); return nullptr; }
+  if (E.ensure_init()) return nullptr;
+  auto *R = new ResidentJob();
+  if (parse_system(s, R->P)) { delete R; return nullptr; }
+  if (R->P.nCentres == 0 || R->P.nPairs == 0) { set_error("job has no units"); delete R; return nullptr; }
+  R->T = E.get_tables({R->P.maxLECP, R->P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
+  if (!R->T || stage_job(E, R->P, R->T, R->B, R->J)) { delete R; return nullptr; }
+  if (cudaStreamSynchronize(E.stream) != cudaSuccess) { set_error("staging failed"); delete R; return nullptr; }
+  return R;
+}
+
+int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  auto *R = (ResidentJob *)vj;
+  if (E.use_schedules(R->T)) return 1;
+  const size_t flushBytes = 256u << 20;
+  if (flushL2 && !E.flush.ensure(flushBytes)) { set_error("flush buffer allocation failed"); return 1; }
+  std::vector<cudaEvent_t> ev(4 * nRuns);
+  for (auto &e : ev) cudaEventCreate(&e);
+  for (int r = 0; r < nRuns; r++) {
+    if (flushL2) cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
+    cudaEventRecord(ev[4 * r], E.stream);
+    if (run_pipeline(E, R->B, R->J, ev[4 * r + 2], ev[4 * r + 3])) return 1;
+    cudaEventRecord(ev[4 * r + 1], E.stream);
+  }
+  cudaError_t ce = cudaStreamSynchronize(E.stream);
+  if (ce != cudaSuccess) { set_error("device error: %s", cudaGetErrorString(ce)); return 1; }
+  for (int r = 0; r < nRuns; r++) {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, ev[4 * r], ev[4 * r + 1]);
+    cudaEventElapsedTime(&b, ev[4 * r + 2], ev[4 * r + 3]);
+    if (msRun) msRun[r] = a;
+    if (msUnit) msUnit[r] = b;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  return 0;
+}
+
+int job_matrix(void *vj, int rowdim, double *I) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  auto *R = (ResidentJob *)vj;
+  size_t mb = sizeof(double) * (size_t)R->P.dim * R->P.dim;
+  std::vector<double> M((size_t)R->P.dim * R->P.dim);
+  cudaMemcpyAsync(M.data(), R->B.mat.p, mb, cudaMemcpyDeviceToHost, E.stream);
+  if (cudaStreamSynchronize(E.stream) != cudaSuccess) { set_error("copy failed"); return 1; }
+  for (int i = 0; i < R->P.dim; i++)
+    for (int j = i; j < R->P.dim; j++) I[(size_t)i * rowdim + j] += M[(size_t)i * R->P.dim + j];
+  return 0;
+}
+
+long long job_units(const void *vj, long long *emitted) {
+  auto *R = (const ResidentJob *)vj;
+  long long n = (long long)R->P.nCentres * R->P.nPairs;
+  if (emitted) {
+    Engine &E = engine();
+    std::lock_guard<std::mutex> lk(E.mu);
+    std::vector<int> st(n);
+    cudaMemcpy(st.data(), R->B.status.p, sizeof(int) * n, cudaMemcpyDeviceToHost);
+    long long c = 0;
+    for (int v : st) c += v == kUnitDone;
+    *emitted = c;
+  }
+  return n;
+}
+
+int job_launches(const void *vj) { return ((const ResidentJob *)vj)->launches; }
+
+void job_free(void *vj) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  cudaStreamSynchronize(E.stream);
+  delete (ResidentJob *)vj;
+}
+
+}  // namespace ecpgb

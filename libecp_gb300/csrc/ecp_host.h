@@ -1,0 +1,105 @@
+// ecp_host.h -- host-side types of the engine (parsed job, device buffers).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "libecp_gb300.h"
+
+namespace ecpgb {
+
+const char *last_error();
+void set_error(const char *fmt, ...);
+
+// Job description parsed from getIntegrals-style arrays.
+struct Parsed {
+  int nAtoms = 0, nShells = 0, nPrims = 0, nCentres = 0, nPairs = 0, dim = 0;
+  int maxLECP = 0, maxLBS = 0, largeGridOrder = 1024;
+  double tol = 1e-12, acc = 1e-14;
+  std::vector<double> geom, primA, primD, termN, termD, termA;
+  std::vector<int> shL, shK, shP, shAtom, shAO, shLocal, atomMaxL, atomShell0;
+  std::vector<int> ctrAtom, ctrL, ctrT0, ctrNT, termL, pairA, pairB;
+  std::vector<long long> pairOff;
+  long long centreStride = 0;
+};
+
+int parse_system(const ecpgb_system &s, Parsed &P);
+
+// Grow-only device buffer.
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t cap = 0;
+  bool ensure(size_t n) {
+    if (n <= cap) return true;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMalloc((void **)&p, n * sizeof(T)) != cudaSuccess) return false;
+    cap = n;
+    return true;
+  }
+  bool upload(const std::vector<T> &v, cudaStream_t s) {
+    if (!ensure(v.size() + 1)) return false;
+    if (!v.empty() && cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return false;
+    return cudaStreamSynchronize(s) == cudaSuccess;
+  }
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+};
+
+// Grow-only pinned host buffer.
+struct PinnedBuf {
+  char *p = nullptr;
+  size_t cap = 0;
+  bool ensure(size_t n) {
+    if (n <= cap) return true;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMallocHost((void **)&p, n) != cudaSuccess) return false;
+    cap = n;
+    return true;
+  }
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf &) = delete;
+  PinnedBuf &operator=(const PinnedBuf &) = delete;
+};
+
+// Device allocations of one job.
+struct JobBuffers {
+  DBuf<char> in;
+  DBuf<double> radius, utab, uL, F, cgeo, usp, ang, out, mat;
+  DBuf<int> gridEnd, win, status, err;
+  PinnedBuf pinned, pinnedOut;
+  int *pinnedErr = nullptr;
+  size_t smem = 0;
+  long long h2dBytes = 0;
+  JobBuffers() { cudaMallocHost((void **)&pinnedErr, 4 * sizeof(int)); }
+  ~JobBuffers() {
+    if (pinnedErr) cudaFreeHost(pinnedErr);
+  }
+};
+
+int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_info *info);
+int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offsets, int *status,
+               ecpgb_info *info, Parsed *parsedOut);
+int layout(const ecpgb_system &s, long long *nUnits, long long *nValues);
+void *job_create(const ecpgb_system &s, int mode);
+int job_run(void *j, int nRuns, int flushL2, float *msRun, float *msUnit);
+int job_matrix(void *j, int rowdim, double *I);
+long long job_units(const void *j, long long *emitted);
+int job_launches(const void *j);
+void job_free(void *j);
+int measure_peaks(double *out);
+
+}  // namespace ecpgb
