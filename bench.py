@@ -1,0 +1,275 @@
+"""Benchmark: ECP shell-pair integrals/s on the batched 50-centre cluster.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (per rank): the batched cluster -- 50 ECP centres (L up to 4, 2-6
+terms per channel), 63 contracted shells (l = 0..3 with weights
+.4/.3/.2/.1, contraction 1..8) giving 2016 shell pairs, i.e. 100,800
+(shell pair, centre) units of which the screening keeps ~91k.  A step is one
+pass of the whole getIntegrals path over that job: shell radii, centre
+potentials, angular tables, F tables, every unit's type-1 and type-2 block,
+and the AO-matrix scatter.  The unit of the metric is one emitted unit (a
+type-1 + type-2 block pair handed to the reference's callback).
+
+value   : device-resident job (inputs in HBM before the timed region); per step
+          CUDA events on the engine's stream; L2 flushed (256 MiB write) between
+          steps, outside the timed spans.
+e2e     : the drop-in getIntegrals call with host buffers: one packed H2D copy
+          of the inputs and a D2H copy of the matrix per step.
+roofline: the per-unit kernel against the measured FP64 FMA pipe (the path is
+          FP64-arithmetic bound; HBM traffic is tiny); algorithmic FLOPs are
+          counted on the oracle's run of the reference control flow over the
+          CPU-baseline sample and scaled per unit.
+Multi-GPU: weak scaling, one independent cluster per rank (seed = rank), no
+          collective on the data path; max over ranks of the timed span.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ECP shell-pair integrals/s"
+UNIT = "integrals/s"
+WORKLOAD = "batched_cluster: 50 ECP centres x 2016 shell pairs (63 shells, l<=3, K 1-8), FP64"
+
+# Algorithmic FLOP weights of the reference control flow:
+# 4 per quadrature point, Bessel 30 per row + 80 per call, exp 20, table 3 per
+# row, 2 per contraction multiply-add.
+def algorithmic_flops(st: dict) -> float:
+    return (4.0 * (st["ps93_points"] + st["psm92_points"]) + 33.0 * st["bessel_rows"]
+            + 80.0 * st["bessel_calls"] + 20.0 * st["exp_calls"] + 2.0 * st["contraction_fma"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if len(r) >= 8 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 8 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows if len(r) >= 8
+                          for n, v in zip(names, r[4:8]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+def cpu_sample_system(system):
+    """Bounded CPU sample: 16 of the 50 centres, basis atoms 0..10 (33 shells)."""
+    from libecp_gb300 import workloads as W  # noqa: F401
+    centres = [a for a in range(system.n_atoms) if system.shellsECP[a] > 0][:16]
+    return system.subset(centres=centres, basis_atoms=range(11)), \
+        "16 of 50 centres x 561 pairs (basis atoms 0-10) of the same cluster"
+
+
+def run_cpu_baseline(system, threads):
+    """Times the reference's CPU path on the sample: oracle/_ref (the unmodified
+    reference) when it loads on this machine, else the oracle restatement.
+    Returns (units/s, kind, stats, sample text)."""
+    from oracle import oracle as O
+    sample, text = cpu_sample_system(system)
+    # the oracle's counters give the algorithmic work of the reference control flow
+    t0 = time.perf_counter()
+    rc, I, st = O.oracle_matrix(sample, nthreads=threads, with_stats=True)
+    t_port = time.perf_counter() - t0
+    units = st["blocks"]
+    kind, t = "port", t_port
+    if O.ref_available():
+        import concurrent.futures as cf
+        centres = [a for a in range(sample.n_atoms) if sample.shellsECP[a] > 0]
+        parts = [sample.subset(centres=centres[i::threads]) for i in range(threads)]
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(O.ref_matrix, parts))
+        t = time.perf_counter() - t0
+        kind = "reference"
+    return units / t, kind, st, text, units, t
+
+
+def make_workload(name, seed):
+    from libecp_gb300 import workloads as W
+    s = W.batched_cluster(seed=seed)
+    if name == "cluster8":
+        s = s.subset(centres=[a for a in range(s.n_atoms) if s.shellsECP[a] > 0][:8])
+    return s
+
+
+def ours(args, rank, world):
+    import libecp_gb300 as eg
+    from libecp_gb300 import workloads as W
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    eg.set_device(local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    system = make_workload(args.workload, rank)
+    peaks = eg.measure_peaks()
+    job = eg.Job(system)
+    job.run(args.warmup, flush_l2=True)
+    n_units, emitted = job.units()
+    if world > 1:
+        dist.barrier()
+        torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms, mu = job.run(args.steps, flush_l2=True)
+    t_step = float(np.mean(ms))
+    t_unit = float(np.mean(mu))
+    if world > 1:
+        t = torch.tensor([t_step, t_unit], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step, t_unit = float(t[0]), float(t[1])
+        e = torch.tensor([float(emitted)], device="cuda", dtype=torch.float64)
+        dist.all_reduce(e)
+        total_units = float(e[0])
+    else:
+        total_units = float(emitted)
+    value = total_units / (t_step / 1e3)
+    launches = job.launches_per_run() * args.steps
+    job.close()
+
+    # end to end through the drop-in getIntegrals with host buffers
+    rc, _, info = eg.get_integrals_info(system)
+    h2d, d2h = info["h2dBytes"], info["d2hBytes"]
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        I = np.zeros((system.dim, system.dim))
+        t0 = time.perf_counter()
+        eg.get_integrals(system, I)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_t.append(dt)
+    e2e_step = float(np.mean(e2e_t))
+    if world > 1:
+        t = torch.tensor([e2e_step], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step = float(t[0])
+    e2e_value = total_units / e2e_step
+
+    line = None
+    if rank == 0:
+        cores = os.cpu_count() or 1
+        cpu_v, kind, st, text, s_units, s_time = run_cpu_baseline(system, min(cores, 16))
+        f_unit = algorithmic_flops(st) / max(st["blocks"], 1)
+        achieved = f_unit * emitted / (t_unit / 1e3) / 1e12
+        peak = peaks["fp64_fma_tflops"]
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "roofline_inputs.json")
+        if os.path.exists(prof):
+            with open(prof) as f:
+                traffic = json.load(f).get("k_unit_dram_bytes_per_launch")
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD if args.workload == "cluster" else WORKLOAD + " [first 8 centres]",
+                       "units_per_rank": int(n_units),
+                       "emitted_units_per_rank": int(emitted), "precision": "fp64 (plain path)",
+                       "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "api": "getIntegrals (host buffers)"},
+            "roofline": {"bound": "fp64", "kernel": "k_unit", "achieved": achieved,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": traffic,
+                         "peak_source": "FP64 FMA pipe measured live by ecpgb_measure_peaks",
+                         "alg_flops_per_unit": f_unit, "unit_kernel_ms": t_unit},
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": min(cores, 16), "kind": kind,
+                             "sample": f"{text}: {s_units} units in {s_time:.1f} s"},
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "peaks_measured": peaks,
+        }
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return line
+
+
+def reference_arm(args, rank, world):
+    """The reference's CPU implementation on this machine's host cores."""
+    if rank != 0:
+        return None
+    from libecp_gb300 import workloads as W
+    from oracle import oracle as O
+    system = W.batched_cluster(seed=0)
+    cores = min(os.cpu_count() or 1, 16)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, kind, st, text, units, t = run_cpu_baseline(system, cores)
+        if i >= args.warmup:
+            vals.append(v)
+    v = float(np.mean(vals))
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * units / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": text,
+                       "note": "reference built from its sources where present, else the C restatement"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": text},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cluster", choices=["cluster", "cluster8"],
+                    help="cluster8: the first 8 centres only (small case for profiler captures)")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.warmup < 3:
+        args.warmup = 3
+    line = reference_arm(args, rank, world) if args.impl == "reference" else ours(args, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

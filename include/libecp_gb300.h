@@ -87,6 +87,10 @@ void ecpgb_job_free(ecpgb_job *j);
  * Takes about 0.5 s.  0 ok. */
 int ecpgb_measure_peaks(double *out);
 
+/* Selects the CUDA device this process's engine uses; call before any other
+ * ecpgb_* or drop-in call (one process per GPU).  0 ok. */
+int ecpgb_set_device(int device);
+
 /* Text of the last error on this thread ("" if none). */
 const char *ecpgb_last_error(void);
 

@@ -86,6 +86,7 @@ def lib() -> ct.CDLL:
     L.ecpgb_job_free.restype = None
     L.ecpgb_measure_peaks.argtypes = [_D]
     L.ecpgb_last_error.restype = ct.c_char_p
+    L.ecpgb_set_device.argtypes = [ct.c_int]
     _lib = L
     return L
 
@@ -263,6 +264,11 @@ class Job:
             self.close()
         except Exception:
             pass
+
+
+def set_device(device: int) -> None:
+    if lib().ecpgb_set_device(int(device)):
+        raise RuntimeError(last_error())
 
 
 def measure_peaks() -> dict:

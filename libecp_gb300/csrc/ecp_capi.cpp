@@ -7,6 +7,8 @@
 // plus the ecpgb_* entry points of libecp_gb300.h.  Every integral is
 // computed by the CUDA kernels; without a GPU the calls fail with an error
 // (there is no CPU path).
+#include <cuda_runtime.h>
+
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -214,6 +216,15 @@ void ecpgb_job_free(ecpgb_job *j) {
 }
 
 int ecpgb_measure_peaks(double *out) { return ecpgb::measure_peaks(out); }
+
+int ecpgb_set_device(int device) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    ecpgb::set_error("cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+    return 1;
+  }
+  return 0;
+}
 
 const char *ecpgb_last_error(void) { return ecpgb::last_error(); }
 

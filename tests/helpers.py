@@ -1,0 +1,55 @@
+"""Shared helpers for the tests (no GPU needed to import)."""
+import os
+from math import gamma, pi
+
+import numpy as np
+
+from libecp_gb300 import workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN_DIR = os.path.join(ROOT, "tests", "golden")
+# Parity bar of the FP64 path against the FP64 reference / oracle.
+TOL_ABS = 1e-10
+
+
+def golden_files():
+    return sorted(f for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+
+
+def load_golden(name):
+    import sys
+    sys.path.insert(0, GOLDEN_DIR)
+    from make_golden import load
+    return load(os.path.join(GOLDEN_DIR, name))
+
+
+def one_centre_system():
+    """ECP and basis on one atom: closed-form answers exist (see one_centre_answers)."""
+    b = W._Builder()
+    ecp = [(0, [(2.0, 3.0, 1.3)]), (1, [(2.0, -2.0, 0.7)]), (2, [(2.0, 1.5, 2.1), (1.0, 0.5, 0.4)])]
+    za, ca, zb, cb = 0.8, 0.6, 1.7, 0.9
+    b.atom([0.0, 0.0, 0.0], ecp=ecp, shells=[(0, [(ca, za)]), (1, [(cb, zb)]), (0, [(cb, zb)])])
+    return b.build("one_centre"), ecp, (za, ca, zb, cb)
+
+
+def one_centre_answers():
+    """<a|U|b> with a, b and U on one centre:
+    4 pi/(2l+1) c_a c_b sum_terms d Gamma((n+2l+1)/2) / (2 p^((n+2l+1)/2)),
+    p = zeta_a + zeta_b + a, over the local terms and the semi-local channel l
+    of the shells (the radial Jacobian r^2 is part of the ECP's r^n)."""
+    _, ecp, (za, ca, zb, cb) = one_centre_system()
+
+    def rad(terms, p0, k):
+        return sum(d * gamma((n + k + 1) / 2) / (2 * (p0 + a) ** ((n + k + 1) / 2))
+                   for n, d, a in terms)
+    loc, ch0, ch1 = ecp[2][1], ecp[0][1], ecp[1][1]
+    return {
+        (0, 0): 4 * pi * ca * ca * (rad(loc, 2 * za, 0) + rad(ch0, 2 * za, 0)),
+        (0, 4): 4 * pi * ca * cb * (rad(loc, za + zb, 0) + rad(ch0, za + zb, 0)),
+        (1, 1): 4 * pi / 3 * cb * cb * (rad(loc, 2 * zb, 2) + rad(ch1, 2 * zb, 2)),
+        (1, 2): 0.0, (0, 1): 0.0,
+    }
+
+
+def max_rel(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
