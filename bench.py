@@ -105,27 +105,47 @@ def cpu_sample_system(system):
         "16 of 50 centres x 561 pairs (basis atoms 0-10) of the same cluster"
 
 
-def run_cpu_baseline(system, threads):
-    """Times the reference's CPU path on the sample: oracle/_ref (the unmodified
-    reference) when it loads on this machine, else the oracle restatement.
-    Returns (units/s, kind, stats, sample text)."""
+_REF_CHILD = """
+import json, sys, time, concurrent.futures as cf
+sys.path.insert(0, {root!r})
+from oracle import oracle as O
+import bench
+from libecp_gb300 import workloads as W
+sample, _ = bench.cpu_sample_system(bench.make_workload({workload!r}, {seed}))
+cs = [a for a in range(sample.n_atoms) if sample.shellsECP[a] > 0]
+parts = [sample.subset(centres=cs[i::{threads}]) for i in range({threads})]
+t0 = time.perf_counter()
+with cf.ThreadPoolExecutor({threads}) as ex:
+    list(ex.map(O.ref_matrix, parts))
+print(json.dumps({{"t": time.perf_counter() - t0}}))
+"""
+
+
+def run_cpu_baseline(system, threads, workload="cluster", seed=0):
+    """Times the reference's CPU path on the sample, on this machine's cores.
+
+    The oracle restatement (kind "port") always runs: its counters give the
+    algorithmic work of the reference's control flow.  Where the unmodified
+    reference was built for this machine (oracle/_ref), it is timed too, in a
+    child process, because it aborts on units whose large-grid quadrature runs
+    out of levels (heap corruption after using a freed table); its time is
+    reported only if it completes.  Returns (units/s, kind, stats, text, units, s).
+    """
     from oracle import oracle as O
     sample, text = cpu_sample_system(system)
-    # the oracle's counters give the algorithmic work of the reference control flow
     t0 = time.perf_counter()
     rc, I, st = O.oracle_matrix(sample, nthreads=threads, with_stats=True)
     t_port = time.perf_counter() - t0
     units = st["blocks"]
     kind, t = "port", t_port
     if O.ref_available():
-        import concurrent.futures as cf
-        centres = [a for a in range(sample.n_atoms) if sample.shellsECP[a] > 0]
-        parts = [sample.subset(centres=centres[i::threads]) for i in range(threads)]
-        t0 = time.perf_counter()
-        with cf.ThreadPoolExecutor(threads) as ex:
-            list(ex.map(O.ref_matrix, parts))
-        t = time.perf_counter() - t0
-        kind = "reference"
+        code = _REF_CHILD.format(root=ROOT, workload=workload, seed=seed, threads=threads)
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+        if r.returncode == 0:
+            kind, t = "reference", json.loads(r.stdout.strip().splitlines()[-1])["t"]
+        else:
+            text += (f"; the unmodified reference aborted on this sample (exit {r.returncode}: "
+                     f"{r.stderr.strip().splitlines()[-1] if r.stderr.strip() else 'no message'})")
     return units / t, kind, st, text, units, t
 
 
@@ -193,7 +213,7 @@ def ours(args, rank, world):
     line = None
     if rank == 0:
         cores = os.cpu_count() or 1
-        cpu_v, kind, st, text, s_units, s_time = run_cpu_baseline(system, min(cores, 16))
+        cpu_v, kind, st, text, s_units, s_time = run_cpu_baseline(system, min(cores, 16), args.workload, rank)
         f_unit = algorithmic_flops(st) / max(st["blocks"], 1)
         achieved = f_unit * emitted / (t_unit / 1e3) / 1e12
         peak = peaks["fp64_fma_tflops"]

@@ -9,9 +9,12 @@
  * (centre C, atom A, atom B >= A, shell s1 of A, shell s2 of B -- s2 >= s1 when
  * A == B -- type-1 block then type-2 block), each IJK(la) x IJK(lb) row-major
  * in libint Cartesian order and freed after the callback returns
- * (src/libecp.c:256-397).  Return value: 0 ok, 1 a type-1 large-grid
- * quadrature did not converge, 2 a type-2 one did not; callbacks stop at the
- * failing block, as the reference's control flow does.
+ * (src/libecp.c:256-397).  Return value: 0 ok; 1 (type 1) or 2 (type 2) when
+ * a large-grid quadrature exhausted its levels -- the reference's codes for an
+ * integration error (src/libecp.h:23-27).  The reference then uses a freed
+ * table and aborts in practice; here that quadrature keeps its full-grid
+ * estimate and every block is still handed out.  -1: engine error (no GPU,
+ * allocation).
  */
 #ifndef LIBECP_H
 #define LIBECP_H 1

@@ -35,17 +35,22 @@ enum {
   ECPGB_FP64 = 0,   /* plain FP64 kernels, one unit per CTA (the drop-in path) */
 };
 
+/* Unit status.  A large-grid (PSM92) quadrature that exhausts its levels keeps
+ * its full-grid estimate and flags the unit; the reference frees its radial
+ * table there and carries on with a dangling pointer (src/type2.c:612-617,
+ * src/type1.c:245-247), which aborts the process in practice. */
 enum {
   ECPGB_UNIT_DONE = 0,
   ECPGB_UNIT_SKIPPED = 1,     /* screened out: no callback in the reference   */
-  ECPGB_UNIT_FAIL_TYPE1 = 2,  /* type-1 large-grid quadrature not converged   */
-  ECPGB_UNIT_FAIL_TYPE2 = 3,  /* type-2 large-grid quadrature not converged   */
+  ECPGB_UNIT_WARN_TYPE1 = 2,  /* blocks written; a type-1 large-grid
+                                 quadrature did not meet its convergence test */
+  ECPGB_UNIT_WARN_TYPE2 = 3,  /* blocks written; the same for type 2 only     */
 };
 
 typedef struct {
   long long units;        /* (pair, centre) units                        */
   long long emitted;      /* units that produced blocks                  */
-  long long firstFailed;  /* first failing unit, -1 if none              */
+  long long firstFailed;  /* first unit with a warning status, -1 if none */
   long long values;       /* doubles in the block layout                 */
   double msGpu;           /* device time of the last run (CUDA events)   */
   double msUnitKernel;    /* of which the per-unit kernel                */
@@ -63,8 +68,8 @@ int ecpgb_blocks(const ecpgb_system *s, int mode, double *values, long long *off
                  int *status, ecpgb_info *info);
 
 /* getIntegrals with a precision mode, a status and timings: returns 0 ok,
- * 1 set-up failed, 2 a large-grid quadrature did not converge (the matrix then
- * holds every block before the failing one, in the reference's order). */
+ * 1 set-up failed, 2 some unit carries a warning status (the matrix holds
+ * every block; see ECPGB_UNIT_WARN_*). */
 int ecpgb_getIntegrals(const ecpgb_system *s, int mode, int rowdim, double *I,
                        ecpgb_info *info);
 

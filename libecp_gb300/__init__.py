@@ -24,7 +24,7 @@ _LL = ct.POINTER(ct.c_longlong)
 _F = ct.POINTER(ct.c_float)
 
 ECPGB_FP64 = 0
-UNIT_DONE, UNIT_SKIPPED, UNIT_FAIL_TYPE1, UNIT_FAIL_TYPE2 = 0, 1, 2, 3
+UNIT_DONE, UNIT_SKIPPED, UNIT_WARN_TYPE1, UNIT_WARN_TYPE2 = 0, 1, 2, 3
 
 
 class EcpgbSystem(ct.Structure):
@@ -157,12 +157,8 @@ def blocks(s: EcpSystem, mode: int = ECPGB_FP64, with_status: bool = False):
         A, s1, la, B, s2, lb, C = units[u]
         n = ncart(la) * ncart(lb)
         o = int(offs[u])
-        if st[u] == UNIT_FAIL_TYPE1:
-            break
         meta.append((A, s1, la, B, s2, lb, C, 1))
         data.append(vals[o:o + n])
-        if st[u] == UNIT_FAIL_TYPE2:
-            break
         meta.append((A, s1, la, B, s2, lb, C, 2))
         data.append(vals[o + n:o + 2 * n])
     meta = np.array(meta, dtype=np.int32).reshape(-1, 8)

@@ -105,6 +105,7 @@ int calculateECPIntegrals(libECPHandle *h, ECPCallback cb, void *args) {
     return -1;
   }
   std::vector<double> blk;
+  int result = 0;
   for (long long u = 0; u < nUnits; u++) {
     int st = status[u];
     if (st == ECPGB_UNIT_SKIPPED) continue;
@@ -113,14 +114,14 @@ int calculateECPIntegrals(libECPHandle *h, ECPCallback cb, void *args) {
     int A = P.shAtom[sa], B = P.shAtom[sb], C = P.ctrAtom[c];
     size_t nb = (size_t)ncart(la) * ncart(lb);
     const double *b1 = values.data() + offsets[u];
-    if (st == ECPGB_UNIT_FAIL_TYPE1) return 1;
     blk.assign(b1, b1 + nb);
     cb(A, P.shLocal[sa], la, 0, B, P.shLocal[sb], lb, 0, C, blk.data(), args);
-    if (st == ECPGB_UNIT_FAIL_TYPE2) return 2;
     blk.assign(b1 + nb, b1 + 2 * nb);
     cb(A, P.shLocal[sa], la, 0, B, P.shLocal[sb], lb, 0, C, blk.data(), args);
+    if (result == 0 && st == ECPGB_UNIT_WARN_TYPE1) result = 1;
+    if (result == 0 && st == ECPGB_UNIT_WARN_TYPE2) result = 2;
   }
-  return 0;
+  return result;
 }
 
 void libECP_free(libECPHandle *h) { delete h; }

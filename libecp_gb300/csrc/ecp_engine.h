@@ -35,9 +35,9 @@ constexpr int kMaxWalkers = 512;       // large-grid quadratures integrated per 
 enum : int {
   kUnitDone = 0,        // both blocks written
   kUnitSkipped = 1,     // screened out: the reference makes no callback
-  kUnitFailType1 = 2,   // a type-1 large-grid quadrature did not converge
-  kUnitFailType2 = 3,   // a type-2 large-grid quadrature did not converge
-  kUnitBadInput = 4,    // sizes beyond what the kernels are compiled for
+  kUnitWarnType1 = 2,   // written; a type-1 large-grid quadrature ran out of levels
+                        // and kept its full-grid estimate (the reference aborts)
+  kUnitWarnType2 = 3,   // written; the same for a type-2 quadrature only
 };
 
 struct DevJob {
@@ -78,7 +78,7 @@ struct DevJob {
   double *out;
   int *status;
   double *mat;
-  int *errWord;          // [0] first failing unit (atomicMin), [1] input error flags
+  int *errWord;          // [0] first unit with a warning (atomicMin), [1] input error flags
 };
 
 // Shared-memory layout of the unit kernel (offsets in doubles).

@@ -599,10 +599,12 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
         if (S.allDone) break;
         s0 = s1;
       }
+      // out of levels: the full-grid estimate stands and the unit is flagged
+      const double Nlast = c92_lvN[c92_nLevels - 1] + 1.0;
       for (int q = tid; q < nf; q += NT) {
         int l1 = S.failIdx[q] & 255, l2 = S.failIdx[q] >> 8;
         if (W.done[q]) Q[l1 * (lab + 1) + l2] += W.res[q];
-        else S.failed = kUnitFailType1;
+        else { Q[l1 * (lab + 1) + l2] += 16 * W.I[q] / (3 * Nlast); S.failed = kUnitWarnType1; }
       }
       __syncthreads();
     }
@@ -838,11 +840,15 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
           if (S.allDone) break;
           s0 = s1;
         }
+        const double Nlast = c92_lvN[c92_nLevels - 1] + 1.0;
         for (int q = tid; q < nf; q += NT) {
           int l, l1, l2, l3;
           item(S.failIdx[q], l, l1, l2, l3);
           if (W.done[q]) T[tidx(l, l1, l2, l3)] += W.res[q];
-          else S.failed = kUnitFailType2;
+          else {
+            T[tidx(l, l1, l2, l3)] += 16 * W.I[q] / (3 * Nlast);
+            if (S.failed == 0) S.failed = kUnitWarnType2;
+          }
         }
         __syncthreads();
       }
@@ -890,28 +896,21 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
 }
 
 // AO matrix, upper triangle: per element the centres' type-1 and type-2
-// contributions in the reference's order (src/getIntegrals.c:36-42); units
-// past the first failing one are not added, as the reference stops there.
+// contributions in the reference's order (src/getIntegrals.c:36-42).
 __global__ void k_scatter(DevJob J) {
   const int pr = blockIdx.x, sa = J.pairA[pr], sb = J.pairB[pr];
   const int la = J.shL[sa], lb = J.shL[sb], na = NCART(la), nb = NCART(lb);
   const int a0 = J.shAO[sa], b0 = J.shAO[sb];
-  const long long firstFail = J.errWord[0];
   for (int e = threadIdx.x; e < na * nb; e += blockDim.x) {
     int i = e / nb, j = e % nb;
     if (a0 + i > b0 + j) continue;
     double acc = 0.0;
     for (int c = 0; c < J.nCentres; c++) {
       long long u = (long long)c * J.nPairs + pr;
-      if (u > firstFail) break;
-      int st = J.status[u];
+      if (J.status[u] == kUnitSkipped) continue;
       const double *o = J.out + (size_t)c * J.centreStride + J.pairOff[pr];
-      if (st == kUnitDone) {
-        acc += o[e];
-        acc += o[na * nb + e];
-      } else if (st == kUnitFailType2) {
-        acc += o[e];
-      }
+      acc += o[e];
+      acc += o[na * nb + e];
     }
     J.mat[(size_t)(a0 + i) * J.dim + b0 + j] += acc;
   }

@@ -427,7 +427,7 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
   for (long long u = 0; u < nUnits; u++) {
     if (status) status[u] = st[u];
     if (offsets) offsets[u] = (u / P.nPairs) * P.centreStride + P.pairOff[u % P.nPairs];
-    emitted += st[u] == kUnitDone;
+    emitted += st[u] != kUnitSkipped;
   }
   int err0 = B.pinnedErr[0], err1 = B.pinnedErr[1];
   if (info) {
@@ -526,7 +526,7 @@ long long job_units(const void *vj, long long *emitted) {
     std::vector<int> st(n);
     cudaMemcpy(st.data(), R->B.status.p, sizeof(int) * n, cudaMemcpyDeviceToHost);
     long long c = 0;
-    for (int v : st) c += v == kUnitDone;
+    for (int v : st) c += v != kUnitSkipped;
     *emitted = c;
   }
   return n;

