@@ -92,6 +92,21 @@ void ecpgb_job_free(ecpgb_job *j);
  * Takes about 0.5 s.  0 ok. */
 int ecpgb_measure_peaks(double *out);
 
+/* getIntegrals for callers that cannot allocate device memory.  No
+ * counterpart in the reference.  Meant for host programs that keep all GPU
+ * memory in their own pool or arena, or that must not pay for (or risk the
+ * failure of) an allocation inside a request.  Same arguments and result as
+ * getIntegrals (accumulates into the upper triangle of I), computed by the
+ * same kernels, but every device buffer comes from one fixed array of
+ * ecpgb_noalloc_capacity() bytes (64 MiB) that each GPU loading the library
+ * holds until the process exits; no CUDA allocation happens.  The first call
+ * on a device looks up that array's address (make it before any stream
+ * capture).  Calls share the array, so calls that overlap on the GPU race.
+ * Returns 0 ok, 1 error (for instance a job larger than the array -- the
+ * message gives the bytes needed), 2 some unit carries a warning status. */
+int ecpgb_getIntegrals_noalloc(const ecpgb_system *s, int rowdim, double *I);
+long long ecpgb_noalloc_capacity(void);
+
 /* Selects the CUDA device this process's engine uses; call before any other
  * ecpgb_* or drop-in call (one process per GPU).  0 ok. */
 int ecpgb_set_device(int device);

@@ -26,6 +26,7 @@ UNITS = [
     ("ecp_peaks.cu", []),
     ("ecp_tables.cpp", []),
     ("ecp_capi.cpp", []),
+    ("ecp_noalloc.cu", []),
 ]
 
 

@@ -238,6 +238,9 @@ static Engine &engine() {
   return *e;
 }
 
+std::mutex &engine_mutex() { return engine().mu; }
+void schedules_overwritten() { engine().schedOwner = nullptr; }
+
 // ------------------------------------------------------------ job set-up
 
 static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "libecp_gb300.h"
@@ -101,5 +102,12 @@ long long job_units(const void *j, long long *emitted);
 int job_launches(const void *j);
 void job_free(void *j);
 int measure_peaks(double *out);
+
+// The engine's lock (serialises every use of the shared __constant__ level
+// schedules), and the notice a caller holding it gives after writing those
+// schedules itself, so the engine re-uploads its own before its next run.
+std::mutex &engine_mutex();
+void schedules_overwritten();
+int run_matrix_noalloc(const ecpgb_system &s, int rowdim, double *I);
 
 }  // namespace ecpgb
