@@ -218,10 +218,12 @@ def ours(args, rank, world):
         achieved = f_unit * emitted / (t_unit / 1e3) / 1e12
         peak = peaks["fp64_fma_tflops"]
         traffic = None
-        prof = os.path.join(ROOT, "profiles", "roofline_inputs.json")
+        prof = os.path.join(ROOT, "profiles", "roofline_inputs.txt")
         if os.path.exists(prof):
             with open(prof) as f:
-                traffic = json.load(f).get("k_unit_dram_bytes_per_launch")
+                per_unit = json.load(f).get("dram_bytes_per_emitted_unit")
+            if per_unit:  # ncu dram read+write of one k_unit launch, scaled to this launch
+                traffic = per_unit * emitted
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
