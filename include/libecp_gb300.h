@@ -33,6 +33,10 @@ typedef struct {
 
 enum {
   ECPGB_FP64 = 0,   /* plain FP64 kernels, one unit per CTA (the drop-in path) */
+  ECPGB_FAST = 1,   /* batched FP64 path: a warp per primitive pair, quadrature
+                       points tabulated level by level until convergence,
+                       Horner-form Bessel rows, table-driven exp; same
+                       schedules and decisions, rounding-level differences */
 };
 
 /* Unit status.  A large-grid (PSM92) quadrature that exhausts its levels keeps

@@ -23,7 +23,8 @@ _I = ct.POINTER(ct.c_int)
 _LL = ct.POINTER(ct.c_longlong)
 _F = ct.POINTER(ct.c_float)
 
-ECPGB_FP64 = 0
+ECPGB_FP64 = 0   # plain FP64 kernels (the drop-in path)
+ECPGB_FAST = 1   # batched FP64 path
 UNIT_DONE, UNIT_SKIPPED, UNIT_WARN_TYPE1, UNIT_WARN_TYPE2 = 0, 1, 2, 3
 
 

@@ -27,6 +27,7 @@ UNITS = [
     ("ecp_tables.cpp", []),
     ("ecp_capi.cpp", []),
     ("ecp_noalloc.cu", []),
+    ("ecp_fast.cu", []),
 ]
 
 

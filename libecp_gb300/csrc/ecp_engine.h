@@ -64,6 +64,9 @@ struct DevJob {
   // tables
   const double *xSmall, *wSmall, *xLarge, *wLarge;
   const double *besT, *besC;
+  const double *besH;          // Taylor coefficients [i][l <= besHL][6] (batched path)
+  int besHL;
+  const double *shNorm;        // spherical-harmonic normalisation [l][m], side tmDim + 1
   const double *p2s, *fac, *dfac;
   const int *atomMaxL;
   const int *ijk, *ijkIdx;
@@ -131,6 +134,21 @@ int upload_schedules(const int *s93slot, int s93n, const int *s93lvEnd, const in
 // Launches the six-kernel pipeline on `stream`; u0/u1 (may be null) are
 // recorded around the per-unit kernel.
 int launch_fp64_pipeline(const DevJob &job, cudaStream_t stream, size_t smemBytes, cudaEvent_t u0,
+                         cudaEvent_t u1);
+// The four per-job kernels before the unit kernel (radii, centre potentials,
+// centre-atom angular tables, windows + F tables) and the AO scatter after it.
+void launch_prologue(const DevJob &job, cudaStream_t stream);
+void launch_epilogue(const DevJob &job, cudaStream_t stream);
+
+// Batched path (ecp_fast.cu): same prologue/epilogue, warp-per-primitive-pair
+// unit kernel with level-granular tabulation, Horner-form Bessel rows and a
+// table-driven exp.  Its level schedules are this unit's own __constant__
+// copies.
+int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, const int *s93lvJ,
+                          const int *s93lvN, int s93levels, const int *s92slot, int s92n,
+                          const int *s92lvEnd, const int *s92lvN, int s92levels, void *stream);
+size_t fast_smem_bytes(int LB, int LE, int nF);
+int launch_fast_pipeline(const DevJob &job, cudaStream_t stream, size_t smemBytes, cudaEvent_t u0,
                          cudaEvent_t u1);
 
 }  // namespace ecpgb

@@ -1,0 +1,820 @@
+// ecp_fast.cu -- batched unit kernel for sm_103a (the fast FP64 path).
+//
+// Same results as the drop-in kernel (same quadrature schedules, windows,
+// convergence tests, stale-buffer semantics of the reference's fallbacks);
+// the work is organised for GB300, where FP64 runs at 1/62 of the FP32 rate
+// and every FP64 operation counts:
+//   * a warp per primitive pair (pairs dealt round-robin to the 4 warps):
+//     no CTA barrier inside the type-1 loop or the type-2 fallback;
+//   * level-granular tabulation: grid points are tabulated 32 schedule slots
+//     at a time (one slot per lane) and a primitive pair stops as soon as all
+//     its quadratures have converged -- the large-grid quadratures converge
+//     after ~27 of 1023 points on average, the reference tabulates all 1023;
+//   * K_l(z) as one Horner pass over precomputed Taylor coefficients (the
+//     reference's 5-step derivative recurrence, done once per table point on
+//     the host); exp by the table-driven method of ecp_fastmath.h;
+//   * the type-1 block accumulated per combined Cartesian index: chi[i][j]
+//     depends on (i, j) only through the index of a_i + b_j
+//     (src/type1.c:323-345), so one accumulator per combined index receives
+//     exactly the terms the reference adds to each chi[i][j].
+#include "ecp_device.cuh"
+#include "ecp_fastmath.h"
+
+namespace ecpgb {
+
+constexpr int kWarps = kUnitThreads / 32;
+constexpr int kWalkCap = 128;  // large-grid quadratures per warp and pass
+
+// --------------------------------------------------------------- helpers
+
+// K_0..K_lmax(z): the branches of src/bessel.c:102-199 with the Taylor branch
+// evaluated from the coefficient table.
+static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *K, int stride) {
+  if (z < 1.0E-7 || z >= 16.0) {
+    bessel_eval(J, lmax, z, K, stride);
+    return;
+  }
+  double h = J.besselN / 16;
+  int index = (int)floor(z * h + 0.5);
+  double dz = z - index / h;
+  const double *c = J.besH + (size_t)index * (J.besHL + 1) * 6;
+  for (int l = 0; l <= lmax; l++) {
+    const double *q = c + 6 * l;
+    double v = fma(q[5], dz, q[4]);
+    v = fma(v, dz, q[3]);
+    v = fma(v, dz, q[2]);
+    v = fma(v, dz, q[1]);
+    K[l * stride] = fma(v, dz, q[0]);
+  }
+}
+
+// One row K_l(z).
+static __device__ double bessel_row(const DevJob &J, int l, double z) {
+  if (z < 1.0E-7 || z >= 16.0) {
+    double K[kMaxRows];
+    bessel_eval(J, l, z, K, 1);
+    return K[l];
+  }
+  double h = J.besselN / 16;
+  int index = (int)floor(z * h + 0.5);
+  double dz = z - index / h;
+  const double *q = J.besH + ((size_t)index * (J.besHL + 1) + l) * 6;
+  double v = fma(q[5], dz, q[4]);
+  v = fma(v, dz, q[3]);
+  v = fma(v, dz, q[2]);
+  v = fma(v, dz, q[1]);
+  return fma(v, dz, q[0]);
+}
+
+// U_l(r) for l = 0..lmax of centre c in one pass over its terms
+// (src/ecp.c:42-60); channels above lmax are skipped.
+static __device__ void channels(const DevJob &J, int c, double r, int lmax, double *U, int stride) {
+  double r2 = r * r;
+  for (int l = 0; l <= lmax; l++) U[l * stride] = 0.0;
+  int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
+  for (int t = t0; t < t1; t++) {
+    int l = J.termL[t];
+    if (l <= lmax) U[l * stride] += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
+  }
+}
+
+static __device__ double channel(const DevJob &J, int c, int l, double r) {
+  double r2 = r * r, pot = 0.0;
+  int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
+  for (int t = t0; t < t1; t++)
+    if (J.termL[t] == l) pot += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
+  return pot;
+}
+
+// FM06 map parameters (src/gc_integrators.c:317-331).
+static __device__ inline void fm06(double za, double zb, double dAC, double dBC, double &i1, double &i2) {
+  double zp = za + zb, P = (za * dAC + zb * dBC) / zp;
+  double sigma = 1.0 / sqrt(zp), t = P - 7.0 * sigma;
+  double rmin = (t > 0.0) ? t : 0.0, rmax = P + 9.0 * sigma;
+  i1 = 0.5 * (rmax - rmin);
+  i2 = 0.5 * (rmax + rmin);
+}
+
+// Schedule steps: step 0 = the head plus 15 (lower, upper) pairs, every later
+// step 16 pairs.  For the large grid step 0 ends exactly at level 3.
+static __device__ inline int step_end93(int s0) { return s0 == 0 ? 33 : s0 + 32; }
+static __device__ inline int step_end92(int s0) { return s0 == 0 ? 31 : s0 + 32; }
+
+// PSM92 walker (src/gc_integrators.c:39-86) over slots [s0, s1) of the
+// large-grid schedule; `val(pos)` = w * f at slot pos; `vis(pos)` whether the
+// (upper) point counts.  State in I, p, q; returns through done/res.
+template <class V, class Vis>
+static __device__ inline void psm92_advance(int s0, int s1, double tol, V val, Vis vis, double &I,
+                                            double &p, double &q, bool &done, double &res) {
+  int pos = s0;
+  if (pos == 0) {
+    I = val(0);
+    p = I;
+    pos = 1;
+  }
+  int k = level_of(pos);
+  while (pos < s1 && !done) {
+    int lvStart = k == 0 ? 1 : c92_lvEnd[k - 1];
+    if (pos == lvStart) {
+      q = 2 * p;
+      p = 2 * I;
+    }
+    double T = 0.0;
+    T += val(pos);
+    if (vis(pos + 1)) T += val(pos + 1);
+    I += T;
+    pos += 2;
+    if (pos == c92_lvEnd[k]) {
+      double N = c92_lvN[k] + 1.0, e = I - p;
+      if (16 * e * e <= 3 * N * fabs(I - q) * tol) {
+        res = 16 * I / (3 * N);
+        done = true;
+      }
+      k++;
+    }
+  }
+}
+
+// --------------------------------------------------------------- layout
+
+// Quadratures per primitive pair in the type-1 block ((l1, l2), l2 = l1,
+// l1-2, ...; src/type1.c:189-202), and primitive pairs packed per warp so
+// that most lanes carry a quadrature.
+__host__ __device__ inline int t1_items(int lab) {
+  int n = 0;
+  for (int l1 = 0; l1 <= lab; l1++) n += l1 / 2 + 1;
+  return n;
+}
+__host__ __device__ inline int t1_group(int lab) {
+  int g = 32 / t1_items(lab);
+  return g > 8 ? 8 : (g < 1 ? 1 : g);
+}
+
+struct FastSmem {
+  int chi, J, T, phase, total;
+  // type-1 per warp (inside phase): pair scalars, S_lm, Q, H, step table
+  int w1Stride, w1Sc, w1Rsh, w1Q, w1H, w1Tab;
+  // type-2: small-grid stage (inside phase)
+  int Fa, Fb;
+  // type-2 fallback per warp (inside phase)
+  int w2Stride, w2Tab, w2I, w2P, w2Q, w2R, w2Part, tab2Stride;
+};
+
+__host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF) {
+  FastSmem s{};
+  const int nA = 2 * LB + 1, nE = LE > 0 ? LE : 1, LBE = LB + nE;
+  const int nc = (LB + 1) * (LB + 2) * (LB + 3) / 6, nct = (LB + 1) * (LB + 2) / 2;
+  const int ncAB = (2 * LB + 1) * (2 * LB + 2) * (2 * LB + 3) / 6;
+  int rq = 0, tt = 0;  // largest per-warp S_lm/Q and step-table widths over lab <= 2 LB
+  for (int lab = 0; lab <= 2 * LB; lab++) {
+    int g = t1_group(lab), lq = lab + 1;
+    if (g * lq * lq > rq) rq = g * lq * lq;
+    if (g * (2 + 2 * lq) > tt) tt = g * (2 + 2 * lq);
+  }
+  int o = 0;
+  s.chi = o; o += nc * nc;
+  s.J = o; o += nct * nc;
+  s.T = o; o += nE * LBE * LBE * nA;
+  s.phase = o;
+  s.w1Sc = 0;
+  s.w1Rsh = 32;
+  s.w1Q = s.w1Rsh + rq;
+  s.w1H = s.w1Q + rq;
+  s.w1Tab = s.w1H + ncAB;
+  s.w1Stride = s.w1Tab + 33 * tt;
+  int t1 = kWarps * s.w1Stride;
+  s.Fa = 0;
+  s.Fb = kSmallOrder * nF;
+  int t2a = 2 * kSmallOrder * nF;
+  // type 2 fallback: 32-slot table (w, base, vis, U[nE], R[nA], Ka[LBE], Kb[LBE]) + walker state
+  s.tab2Stride = 3 + nE + nA + 2 * LBE;
+  s.w2Tab = 0;
+  s.w2I = 32 * s.tab2Stride;
+  s.w2P = s.w2I + kWalkCap;
+  s.w2Q = s.w2P + kWalkCap;
+  s.w2R = s.w2Q + kWalkCap;
+  s.w2Part = s.w2R + kWalkCap;
+  s.w2Stride = s.w2Part + kWalkCap;
+  int t2b = kWarps * s.w2Stride;
+  int ph = t1;
+  if (t2a > ph) ph = t2a;
+  if (t2b > ph) ph = t2b;
+  s.total = s.phase + ph;
+  return s;
+}
+
+size_t fast_smem_bytes(int LB, int LE, int nF) { return sizeof(double) * (size_t)fast_layout(LB, LE, nF).total; }
+
+struct FastShared {
+  int ppBreak[kMaxContraction * kMaxContraction];
+  int failIdx[kWalkCap];
+  unsigned failMask[64];
+  int nFail, nThis, nextBase;
+  int warn;
+};
+
+// --------------------------------------------------------------- type 1
+
+// Column m of the real spherical harmonics S_lm, l = m..lmax, into rsh[l*l +
+// l -/+ m]: the associated Legendre recurrence, normalisation and sin/cos(m
+// phi) recurrence of src/spherical_harmonics.c:16-114, one column per lane.
+static __device__ void rsh_column(const DevJob &J, int lmax, int m, double theta, double phi,
+                                  double *rsh) {
+  const int W = J.tmDim + 1;
+  double sm = 0.0, cm = 1.0;
+  if (m > 0 && phi != 0.0) {
+    double s1 = sin(phi), c1 = cos(phi);
+    sm = s1;
+    cm = c1;
+    for (int i = 2; i <= m; i++) {
+      double sn = s1 * cm + c1 * sm, cn = c1 * cm - s1 * sm;
+      sm = sn;
+      cm = cn;
+    }
+  }
+  double x = cos(theta), P2 = 0.0, P1 = 0.0, P = 0.0;
+  double sp = 1.0;
+  if (x != 1.0 && x != -1.0) {
+    double s1 = sqrt(1.0 - x * x);
+    sp = s1;
+    for (int i = 2; i <= m; i++) sp = sp * s1;
+  }
+  for (int l = m; l <= lmax; l++) {
+    if (1.0 == x) P = (m == 0) ? 1.0 : 0.0;
+    else if (-1.0 == x) P = (m == 0) ? (l == 0 ? 1.0 : -P1) : 0.0;
+    else if (l == m) P = (m == 0) ? 1.0 : sp * J.dfac[2 * m - 1];
+    else if (l == m + 1) P = x * (2 * m + 1) * P1;
+    else P = (x * (2 * l - 1) * P1 - (l + m - 1) * P2) / (l - m);
+    P2 = P1;
+    P1 = P;
+    double v = J.shNorm[l * W + m] * P;
+    if (m == 0) rsh[l * l + l] = v / sqrt(2.0);
+    else {
+      rsh[l * l + l - m] = v * sm;
+      rsh[l * l + l + m] = v * cm;
+    }
+  }
+}
+
+// A group of G primitive pairs (p0 .. p0+G-1) of the type-1 block, by one
+// warp (src/type1.c:95-302); lane = (pair, quadrature).  Adds the group's terms
+// to the warp's per-combined-index accumulators H.
+static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *W, int c, int Lc,
+                                    int la, int lb, int p0, int G, int Nb, const double *pzA,
+                                    const double *pcA, const double *pzB, const double *pcB,
+                                    const double *gA, const double *gB, int ws, int we, int &warn) {
+  const int lane = threadIdx.x & 31, lab = la + lb, lq = lab + 1, O = kSmallOrder;
+  const int OL = J.largeOrder, TSl = 2 + 2 * lq, RQ = lq * lq, nq = t1_items(lab);
+  double *sc = W + L.w1Sc, *rsh = W + L.w1Rsh, *Q = W + L.w1Q, *H = W + L.w1H, *tab = W + L.w1Tab;
+  const double dAC = gA[3], dBC = gB[3];
+  const double *uL = J.uL + (size_t)c * O;
+  // (1) per pair: k-vector, its spherical coordinates, the prefactor
+  if (lane < G) {
+    int k = p0 + lane;
+    double za = pzA[k / Nb], ca = pcA[k / Nb], zb = pzB[k % Nb], cb = pcB[k % Nb];
+    double P[3], Sp[3];
+    for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * gA[i] + zb * gB[i]);
+    to_spherical(P, Sp);
+    sc[lane * 4 + 0] = Sp[0];
+    sc[lane * 4 + 1] = Sp[1];
+    sc[lane * 4 + 2] = Sp[2];
+    sc[lane * 4 + 3] = ca * cb * fast_exp(-za * dAC * dAC - zb * dBC * dBC);
+  }
+  __syncwarp();
+  // (2) S_lm of every pair, one (pair, m) column per lane
+  if (lane < G * lq) {
+    int g = lane / lq, m = lane % lq;
+    rsh_column(J, lab, m, sc[g * 4 + 1], sc[g * 4 + 2], rsh + g * RQ);
+  }
+  for (int e = lane; e < G * RQ; e += 32) Q[e] = 0.0;
+  __syncwarp();
+  // (3) small grid, PS93: lane = (pair g, quadrature (l1, l2))
+  const bool mine = lane < G * nq;
+  const int g = mine ? lane / nq : 0;
+  int l1 = 0, l2 = 0;
+  {
+    int rem = mine ? lane % nq : 0;
+    while (l1 <= lab && rem >= l1 / 2 + 1) { rem -= l1 / 2 + 1; l1++; }
+    l2 = l1 - 2 * rem;
+  }
+  double I = 0, p = 0, q = 0, err = 0;
+  bool done = !mine;
+  int k = 0, cnt = 0;
+  for (int s0 = 0; s0 < O;) {
+    const int s1 = step_end93(s0) < O ? step_end93(s0) : O;
+    for (int e = lane; e < (s1 - s0) * G; e += 32) {
+      const int t = s0 + e / G, gg = e % G, kk = p0 + gg, n = c93_slot[t];
+      double *ent = tab + e * TSl;
+      ent[0] = J.wSmall[n];
+      if (n >= ws && n < we) {
+        const double za = pzA[kk / Nb], zb = pzB[kk % Nb], s = sc[gg * 4];
+        double r = J.xSmall[n], ex = ((-za - zb) * r + s) * r;
+        ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
+        ent[1] = sc[gg * 4 + 3] * uL[n] * ex;
+        bessel_fast(J, lab, s * r, ent + 2, 1);
+        double *R = ent + 2 + lq;
+        R[0] = 1.0;
+        for (int l = 1; l <= lab; l++) R[l] = r * R[l - 1];
+      } else {
+        for (int l = 1; l < TSl; l++) ent[l] = 0.0;
+      }
+    }
+    __syncwarp();
+    auto val = [&](int t) {
+      const double *e = tab + ((t - s0) * G + g) * TSl;
+      return e[0] * (e[1] * e[2 + lq + l1] * e[2 + l2]);
+    };
+    int t = s0;
+    if (t == 0) {
+      if (!done) {
+        p = val(0);
+        q = val(1) + val(2);
+        I = p + q;
+      }
+      t = 3;
+    }
+    while (t < s1) {
+      int lvStart = k == 0 ? 3 : c93_lvEnd[k - 1];
+      if (t == lvStart) cnt = 0;
+      int lo = c93_slot[t], hi = c93_slot[t + 1];
+      double T = 0.0;
+      if (lo >= ws) { if (!done) T += val(t); cnt++; }
+      if (hi <= we) { if (!done) T += val(t + 1); cnt++; }
+      if (!done) I += T;
+      t += 2;
+      if (t == c93_lvEnd[k]) {
+        int j = c93_lvJ[k], n = c93_lvN[k];
+        if (!done) {
+          p += (1 - j) * (I - q);
+          if (cnt > 0) err = 16 * fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q)) / (3 * n);
+          q = (1 - j) * q + j * I;
+          if (cnt > 0 && err < J.tol) {
+            done = true;
+            Q[g * RQ + l1 * lq + l2] += 16 * q / (3 * n);
+          }
+        }
+        k++;
+      }
+    }
+    __syncwarp();
+    s0 = s1;
+    if (__all_sync(0xffffffffu, done)) break;
+  }
+  // (4) large-grid fallback, one pair of the group at a time, for the
+  //     quadratures that did not converge (src/type1.c:149-196)
+  const bool failed = mine && !done;
+  for (int gg = 0; gg < G; gg++) {
+    const bool fail = failed && g == gg;
+    if (!__ballot_sync(0xffffffffu, fail)) continue;
+    const int kk = p0 + gg;
+    const double za = pzA[kk / Nb], ca = pcA[kk / Nb], zb = pzB[kk % Nb], cb = pcB[kk % Nb];
+    const double s = sc[gg * 4], z = -za - zb, zd2 = -za * dAC * dAC - zb * dBC * dBC;
+    const double C2 = ca * cb;
+    double i1, i2;
+    fm06(za, zb, dAC, dBC, i1, i2);
+    int nb = OL;  // first point past both centres whose exponent is below the screen
+    for (int n0 = 0; n0 < OL; n0 += 32) {
+      int n = n0 + lane;
+      bool pr = false;
+      if (n < OL) {
+        double r = i1 * J.xLarge[n] + i2, e = (z * r + s) * r + zd2;
+        pr = r > dAC && r > dBC && e < J.lnAcc1;
+      }
+      unsigned b = __ballot_sync(0xffffffffu, pr);
+      if (b) { nb = n0 + __ffs(b) - 1; break; }
+    }
+    const int end = nb - 1;
+    double I2 = 0, p2 = 0, q2 = 0, res2 = 0;
+    bool done2 = !fail;
+    for (int s0 = 0; s0 < OL;) {
+      const int s1 = step_end92(s0) < OL ? step_end92(s0) : OL;
+      for (int t = s0 + lane; t < s1; t += 32) {
+        int n = c92_slot[t];
+        bool upper = t > 0 && ((t - 1) & 1);
+        double *e = tab + (t - s0) * TSl;
+        double *K = e + 2, *R = e + 2 + lq;
+        e[0] = J.wLarge[n] * i1;
+        e[1] = 0.0;
+        if (n < nb) {
+          double r = i1 * J.xLarge[n] + i2, ex = (z * r + s) * r + zd2;
+          if (ex >= J.lnAcc1) {
+            e[1] = C2 * channel(J, c, Lc, r) * fast_exp(ex);
+            bessel_fast(J, lab, s * r, K, 1);
+            R[0] = 1.0;
+            for (int l = 1; l <= lab; l++) R[l] = r * R[l - 1];
+          }
+        } else if (n != nb && !upper && n < O && n >= ws && n < we) {
+          // beyond the break the reference integrates its small-grid buffers:
+          // exponent and U_L at index n, r^l and K_l at flat offset l*OL + n of
+          // rows written with the small grid's stride
+          double rs = J.xSmall[n], es = (z * rs + s) * rs;
+          if (es >= J.lnAcc1) {
+            e[1] = C2 * uL[n] * fast_exp(es);
+            for (int l = 0; l <= lab; l++) {
+              int f = l * OL + n, lr = f / O, nr = f % O;
+              bool ok = lr <= lab && nr >= ws && nr < we;
+              double xr = J.xSmall[nr], pw = 1.0;
+              for (int i = 0; i < lr && ok; i++) pw = xr * pw;
+              R[l] = ok ? pw : 0.0;
+              K[l] = ok ? bessel_row(J, lr, s * xr) : 0.0;
+            }
+          }
+        }
+        if (upper && n > end) e[1] = 0.0;
+      }
+      __syncwarp();
+      if (!done2) {
+        auto val = [&](int t) {
+          const double *e = tab + (t - s0) * TSl;
+          return e[1] == 0.0 ? 0.0 : e[0] * (e[1] * e[2 + lq + l1] * e[2 + l2]);
+        };
+        auto vis = [&](int t) { return c92_slot[t] <= end; };
+        psm92_advance(s0, s1, J.tol, val, vis, I2, p2, q2, done2, res2);
+      }
+      __syncwarp();
+      s0 = s1;
+      if (__all_sync(0xffffffffu, done2)) break;
+    }
+    if (fail) {
+      if (!done2) {
+        res2 = 16 * I2 / (3 * (c92_lvN[c92_nLevels - 1] + 1.0));
+        warn = 1;
+      }
+      Q[g * RQ + l1 * lq + l2] += res2;
+    }
+    __syncwarp();
+  }
+  __syncwarp();
+  // (5) H[p] += sum_l (sum_m S_lm poly2sph[p][lm]) Q[|p|][l], pair by pair in
+  //     order (src/type1.c:323-345)
+  const int dd = J.tmDim + 1, tmW = (J.tmDim + 1) * (J.tmDim + 1);
+  const int ncab = (lab + 1) * (lab + 2) * (lab + 3) / 6;
+  for (int pi = lane; pi < ncab; pi += 32) {
+    const int *ex = J.ijk + 3 * pi;
+    const int lmax = ex[0] + ex[1] + ex[2];
+    const int prow = J.ijkIdx[(ex[0] * dd + ex[1]) * dd + ex[2]];
+    double acc = H[pi];
+    for (int gg = 0; gg < G; gg++) {
+      const double *rs = rsh + gg * RQ, *Qg = Q + gg * RQ;
+      for (int l = lmax; l >= 0; l -= 2) {
+        double factor = 0.0;
+        for (int m = 0; m < 2 * l + 1; m++) factor += rs[l * l + m] * J.p2s[(size_t)prow * tmW + l * l + m];
+        acc += factor * Qg[lmax * lq + l];
+      }
+    }
+    H[pi] = acc;
+  }
+  __syncwarp();
+}
+
+// --------------------------------------------------------------- type 2
+
+// One primitive pair of the type-2 large-grid fallback, by one warp
+// (src/type2.c:418-528): integrates the pass's failed items and adds each
+// result to the warp's partial sums.
+static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, const FastShared &S,
+                               int k, int Nb, int nf, int c, int Lc, int la, int lb, const double *pzA,
+                               const double *pcA, const double *pzB, const double *pcB, double dAC,
+                               double dBC, int ncls, int &warn) {
+  const int lane = threadIdx.x & 31, lab = la + lb, nA = 2 * J.maxLBS + 1;
+  const int LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE, OL = J.largeOrder;
+  const int TS = L.tab2Stride, laC = la + Lc - 1, lbC = lb + Lc - 1;
+  double *tab = W + L.w2Tab, *sI = W + L.w2I, *sP = W + L.w2P, *sQ = W + L.w2Q, *sR = W + L.w2R;
+  double *part = W + L.w2Part;
+  const double za = pzA[k / Nb], ca = pcA[k / Nb], zb = pzB[k % Nb], cb = pcB[k % Nb];
+  const double Ck = ca * cb;
+  double i1, i2;
+  fm06(za, zb, dAC, dBC, i1, i2);
+  const int nb = S.ppBreak[k], end = nb == INT_MAX ? OL - 1 : nb - 1;
+  for (int q = lane; q < nf; q += 32) { sI[q] = 0; sP[q] = 0; sQ[q] = 0; sR[q] = 0; }
+  __syncwarp();
+  unsigned doneBits[kWalkCap / 32] = {0u, 0u, 0u, 0u};
+  for (int s0 = 0; s0 < OL;) {
+    const int s1 = step_end92(s0) < OL ? step_end92(s0) : OL;
+    for (int t = s0 + lane; t < s1; t += 32) {
+      int n = c92_slot[t];
+      bool upper = t > 0 && ((t - 1) & 1);
+      double *e = tab + (t - s0) * TS;
+      double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
+      e[0] = J.wLarge[n] * i1;
+      e[1] = 0.0;
+      e[2] = (!upper || n <= end) ? 1.0 : 0.0;
+      int owner = -1;
+      if (n < nb) owner = k;
+      else if (n != nb && !upper) {
+        for (int j = k - 1; j >= 0; j--)
+          if (S.ppBreak[j] >= n) { owner = j; break; }
+        if (owner >= 0 && S.ppBreak[owner] == n) owner = -1;
+      }
+      if (owner >= 0) {
+        const double zaj = pzA[owner / Nb], zbj = pzB[owner % Nb];
+        double i1j = i1, i2j = i2;
+        if (owner != k) fm06(zaj, zbj, dAC, dBC, i1j, i2j);
+        double r = i1j * J.xLarge[n] + i2j, d1 = dAC - r, d2 = dBC - r;
+        double ex = -zaj * d1 * d1 - zbj * d2 * d2;
+        if (ex >= J.lnAcc2) {
+          e[1] = Ck * fast_exp(ex);
+          channels(J, c, r, Lc - 1, U, 1);
+          bessel_fast(J, laC, 2.0 * zaj * dAC * r, Ka, 1);
+          bessel_fast(J, lbC, 2.0 * zbj * dBC * r, Kb, 1);
+          R[0] = 1.0;
+          for (int l = 1; l <= lab; l++) R[l] = r * R[l - 1];
+        }
+      }
+    }
+    __syncwarp();
+    bool all = true;
+    for (int q = lane, qi = 0; q < nf; q += 32, qi++) {
+      if (doneBits[qi] & (1u << lane)) continue;
+      int v = S.failIdx[q], l = 0, qq = v;
+      while (qq >= J.itemCnt[ncls + l]) { qq -= J.itemCnt[ncls + l]; l++; }
+      int it = J.items[J.itemOff[ncls + l] + qq];
+      int l1 = it & 255, l2 = (it >> 8) & 255, l3 = it >> 16;
+      auto val = [&](int t) {
+        const double *e = tab + (t - s0) * TS;
+        if (e[1] == 0.0) return 0.0;
+        const double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
+        return e[0] * (e[1] * U[l] * R[l3] * Ka[l1] * Kb[l2]);
+      };
+      auto vis = [&](int t) { return tab[(t - s0) * TS + 2] != 0.0; };
+      double I = sI[q], p = sP[q], qv = sQ[q], res = 0;
+      bool done = false;
+      psm92_advance(s0, s1, J.tol, val, vis, I, p, qv, done, res);
+      sI[q] = I; sP[q] = p; sQ[q] = qv;
+      if (done) { sR[q] = res; doneBits[qi] |= 1u << lane; }
+      else all = false;
+    }
+    __syncwarp();
+    s0 = s1;
+    if (__all_sync(0xffffffffu, all)) break;
+  }
+  const double Nlast = c92_lvN[c92_nLevels - 1] + 1.0;
+  for (int q = lane, qi = 0; q < nf; q += 32, qi++) {
+    if (doneBits[qi] & (1u << lane)) part[q] += sR[q];
+    else { part[q] += 16 * sI[q] / (3 * Nlast); warn = 1; }
+  }
+  __syncwarp();
+}
+
+// --------------------------------------------------------------- the kernel
+
+__global__ void __launch_bounds__(kUnitThreads) k_unit_fast(DevJob J) {
+  extern __shared__ double sm[];
+  __shared__ FastShared S;
+  const long long u = blockIdx.x;
+  const int c = (int)(u / J.nPairs), pr = (int)(u % J.nPairs);
+  const int sa = J.pairA[pr], sb = J.pairB[pr], tid = threadIdx.x, NT = blockDim.x;
+  const int warp = tid >> 5;
+  const int *wa = J.win + ((size_t)c * J.nShells + sa) * 3;
+  const int *wb = J.win + ((size_t)c * J.nShells + sb) * 3;
+  if (wa[2] || wb[2]) {
+    if (tid == 0) J.status[u] = kUnitSkipped;
+    return;
+  }
+  const int ws = wa[0] > wb[0] ? wa[0] : wb[0];
+  const int we = wa[1] > wb[1] ? wa[1] : wb[1];
+  if (!(ws < we)) {
+    if (tid == 0) J.status[u] = kUnitSkipped;
+    return;
+  }
+  const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.nF);
+  const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa], lb = J.shL[sb], lab = la + lb;
+  const int nA = 2 * J.maxLBS + 1, LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE;
+  const int Lc = J.ctrL[c], nca = NCUM(la), ncb = NCUM(lb), O = kSmallOrder;
+  const size_t cA = (size_t)c * J.nAtoms + A, cB = (size_t)c * J.nAtoms + B;
+  const double *gA = J.cgeo + cA * 4, *gB = J.cgeo + cB * 4;
+  const double dAC = gA[3], dBC = gB[3];
+  const double *pzA = J.primA + J.shP[sa], *pcA = J.primD + J.shP[sa];
+  const double *pzB = J.primA + J.shP[sb], *pcB = J.primD + J.shP[sb];
+  const int Na = J.shK[sa], Nb = J.shK[sb], NP = Na * Nb;
+  double *chi = sm + Lm.chi, *Jsh = sm + Lm.J, *T = sm + Lm.T, *ph = sm + Lm.phase;
+  double *out1 = J.out + (size_t)c * J.centreStride + J.pairOff[pr];
+  double *out2 = out1 + NCART(la) * NCART(lb);
+  int warn1 = 0, warn2 = 0;
+  if (tid == 0) S.warn = 0;
+
+  // ---------------------------------------------------------- type 1
+  {
+    double *W = ph + warp * Lm.w1Stride;
+    const int ncab = (lab + 1) * (lab + 2) * (lab + 3) / 6;
+    for (int e = tid & 31; e < ncab; e += 32) W[Lm.w1H + e] = 0.0;
+    __syncwarp();
+    const int G = t1_group(lab);
+    for (int p0 = warp * G; p0 < NP; p0 += kWarps * G)
+      t1_group_run(J, Lm, W, c, Lc, la, lb, p0, NP - p0 < G ? NP - p0 : G, Nb, pzA, pcA, pzB, pcB, gA, gB,
+                   ws, we, warn1);
+    __syncthreads();
+    // chi[i][j] = sum over warps of H[index(a_i + b_j)]
+    const int dd = J.tmDim + 1;
+    for (int e = tid; e < nca * ncb; e += NT) {
+      const int *ei = J.ijk + 3 * (e / ncb), *ej = J.ijk + 3 * (e % ncb);
+      int pi = J.ijkIdx[((ei[0] + ej[0]) * dd + (ei[1] + ej[1])) * dd + ei[2] + ej[2]];
+      double v = 0.0;
+      for (int w = 0; w < kWarps; w++) v += ph[w * Lm.w1Stride + Lm.w1H + pi];
+      chi[e] = v;
+    }
+    __syncthreads();
+  }
+  auto poly_shift = [&](double norm, double *dst) {  // src/util.c:247-334
+    const int D = J.uspD, dd = J.tmDim + 1, nta = NCART(la), ntb = NCART(lb);
+    const double *uA = J.usp + cA * D * D * D, *uB = J.usp + cB * D * D * D;
+    for (int e = tid; e < nta * ncb; e += NT) {
+      int c1 = e / ncb, q = e % ncb;
+      const int *ex = J.ijk + 3 * (NCUM(la - 1) + c1);
+      double v = 0.0;
+      for (int x = 0; x <= ex[0]; x++) {
+        double bx = binom(J.fac, ex[0], x);
+        for (int y = 0; y <= ex[1]; y++) {
+          double by = bx * binom(J.fac, ex[1], y);
+          for (int zz = 0; zz <= ex[2]; zz++) {
+            double bz = by * binom(J.fac, ex[2], zz);
+            double factor = bz * uA[((ex[0] - x) * D + (ex[1] - y)) * D + (ex[2] - zz)];
+            if (fabs(factor) <= J.acc) continue;
+            v += factor * chi[J.ijkIdx[(x * dd + y) * dd + zz] * ncb + q];
+          }
+        }
+      }
+      Jsh[e] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < nta * ntb; e += NT) {
+      int c1 = e / ntb, c2 = e % ntb;
+      const int *ex = J.ijk + 3 * (NCUM(lb - 1) + c2);
+      double v = 0.0;
+      for (int x = 0; x <= ex[0]; x++) {
+        double bx = binom(J.fac, ex[0], x);
+        for (int y = 0; y <= ex[1]; y++) {
+          double by = bx * binom(J.fac, ex[1], y);
+          for (int zz = 0; zz <= ex[2]; zz++) {
+            double bz = by * binom(J.fac, ex[2], zz);
+            double factor = bz * uB[((ex[0] - x) * D + (ex[1] - y)) * D + (ex[2] - zz)];
+            if (fabs(factor) <= J.acc) continue;
+            factor *= norm;
+            v += factor * Jsh[c1 * ncb + J.ijkIdx[(x * dd + y) * dd + zz]];
+          }
+        }
+      }
+      dst[e] = v;
+    }
+    __syncthreads();
+  };
+  const double norm1 = 4.0 * kPi, norm2 = norm1 * norm1;
+  poly_shift(norm1, out1);
+
+  // ---------------------------------------------------------- type 2
+  const int nF = J.nF;
+  double *Fa = ph + Lm.Fa, *Fb = ph + Lm.Fb;
+  const double *gFa = J.F + ((size_t)c * J.nShells + sa) * O * nF;
+  const double *gFb = J.F + ((size_t)c * J.nShells + sb) * O * nF;
+  for (int e = tid; e < O * nF; e += NT) { Fa[e] = gFa[e]; Fb[e] = gFb[e]; }
+  for (int e = tid; e < LE * LBE * LBE * nA; e += NT) T[e] = 0.0;
+  for (int e = tid; e < 64; e += NT) S.failMask[e] = 0;
+  if (tid == 0) S.nFail = 0;
+  __syncthreads();
+  const double *Ut = J.utab + (size_t)c * O * LE * J.nk;
+  const int ncls = (la * (J.maxLBS + 1) + lb) * LE;
+  int nItems = 0;
+  for (int l = 0; l < Lc; l++) nItems += J.itemCnt[ncls + l];
+  auto item = [&](int q, int &l, int &l1, int &l2, int &l3) {
+    l = 0;
+    while (q >= J.itemCnt[ncls + l]) { q -= J.itemCnt[ncls + l]; l++; }
+    int v = J.items[J.itemOff[ncls + l] + q];
+    l1 = v & 255; l2 = (v >> 8) & 255; l3 = v >> 16;
+  };
+  auto tidx = [&](int l, int l1, int l2, int l3) { return ((l * LBE + l1) * LBE + l2) * nA + l3; };
+  for (int q = tid; q < nItems; q += NT) {  // small-grid PS93 (src/type2.c:337-387)
+    int l, l1, l2, l3;
+    item(q, l, l1, l2, l3);
+    const int nk = J.nk;
+    double res;
+    bool ok = ps93_walk(J.wSmall, ws, we, J.tol,
+                        [&](int n) {
+                          return Fa[n * nF + l1] * Fb[n * nF + l2] * Ut[((size_t)n * LE + l) * nk + l3];
+                        },
+                        res);
+    if (ok) T[tidx(l, l1, l2, l3)] = res;
+    else { atomicOr(&S.failMask[q >> 5], 1u << (q & 31)); atomicAdd(&S.nFail, 1); }
+  }
+  __syncthreads();
+  if (S.nFail > 0) {
+    // break index of every primitive pair (bisection: the break predicate is
+    // monotone in the index beyond both centres)
+    for (int k = tid; k < NP; k += NT) {
+      double za = pzA[k / Nb], zb = pzB[k % Nb], i1, i2;
+      fm06(za, zb, dAC, dBC, i1, i2);
+      int lo = 0, hi = J.largeOrder;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        double r = i1 * J.xLarge[mid] + i2, d1 = dAC - r, d2 = dBC - r;
+        double e = -za * d1 * d1 - zb * d2 * d2;
+        if (r > dAC && r > dBC && e < J.lnAcc2) hi = mid; else lo = mid + 1;
+      }
+      S.ppBreak[k] = lo < J.largeOrder ? lo : INT_MAX;
+    }
+    if (tid == 0) S.nextBase = 0;
+    __syncthreads();
+    while (S.nextBase < nItems) {
+      if (tid == 0) {
+        int nf = 0, q = S.nextBase;
+        for (; q < nItems && nf < kWalkCap; q++)
+          if (S.failMask[q >> 5] & (1u << (q & 31))) S.failIdx[nf++] = q;
+        S.nThis = nf;
+        S.nextBase = q;
+      }
+      __syncthreads();
+      const int nf = S.nThis;
+      double *W = ph + warp * Lm.w2Stride;
+      for (int q = tid & 31; q < nf; q += 32) W[Lm.w2Part + q] = 0.0;
+      __syncwarp();
+      for (int k = warp; k < NP; k += kWarps)
+        t2_pair(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, warn2);
+      __syncthreads();
+      for (int q = tid; q < nf; q += NT) {
+        double v = 0.0;
+        for (int w = 0; w < kWarps; w++) v += ph[w * Lm.w2Stride + Lm.w2Part + q];
+        int l, l1, l2, l3;
+        item(S.failIdx[q], l, l1, l2, l3);
+        T[tidx(l, l1, l2, l3)] = v;
+      }
+      __syncthreads();
+    }
+  }
+  // gamma (src/type2.c:583-623)
+  {
+    const double *angA = J.ang + cA * J.angLam * J.angLM * J.angC;
+    const double *angB = J.ang + cB * J.angLam * J.angLM * J.angC;
+    const int LMd = J.angLM, AC = J.angC;
+    for (int e = tid; e < nca * ncb; e += NT) {
+      int pidx = e / ncb, qidx = e % ncb, alpha = 0, beta = 0;
+      while (NCUM(alpha) <= pidx) alpha++;
+      while (NCUM(beta) <= qidx) beta++;
+      double g = 0.0;
+      for (int l = 0; l < Lc; l++) {
+        int ll1 = l - alpha, p1 = (alpha + l) % 2;
+        if (p1 > ll1) ll1 = p1;
+        int ll2 = l - beta, p2 = (beta + l) % 2;
+        if (p2 > ll2) ll2 = p2;
+        double tmp = 0.0;
+        for (int l1 = ll1; l1 <= la + l; l1 += 2)
+          for (int l2 = ll2; l2 <= lb + l; l2 += 2) {
+            double factor = 0.0;
+            for (int m = 0; m < 2 * l + 1; m++)
+              factor += angA[((size_t)l1 * LMd + l * l + m) * AC + pidx] * angB[((size_t)l2 * LMd + l * l + m) * AC + qidx];
+            tmp += factor * T[tidx(l, l1, l2, alpha + beta)];
+          }
+        g += tmp;
+      }
+      chi[e] = g;
+    }
+  }
+  __syncthreads();
+  poly_shift(norm2, out2);
+  if (warn1) atomicOr(&S.warn, 1);
+  if (warn2) atomicOr(&S.warn, 2);
+  __syncthreads();
+  if (tid == 0) {
+    int st = (S.warn & 1) ? kUnitWarnType1 : (S.warn & 2) ? kUnitWarnType2 : kUnitDone;
+    J.status[u] = st;
+    if (st != kUnitDone) atomicMin(&J.errWord[0], (int)u);
+  }
+}
+
+// --------------------------------------------------------------- launchers
+
+int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, const int *s93lvJ,
+                          const int *s93lvN, int s93levels, const int *s92slot, int s92n,
+                          const int *s92lvEnd, const int *s92lvN, int s92levels, void *stream) {
+  if (s93n > kSmallOrder || s92n > kMaxLargeOrder || s93levels > 32 || s92levels > 32) return 1;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemcpyToSymbolAsync(c93_slot, s93slot, sizeof(int) * s93n, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c93_lvEnd, s93lvEnd, sizeof(int) * s93levels, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c93_lvJ, s93lvJ, sizeof(int) * s93levels, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c93_lvN, s93lvN, sizeof(int) * s93levels, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c93_nLevels, &s93levels, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c92_slot, s92slot, sizeof(int) * s92n, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c92_lvEnd, s92lvEnd, sizeof(int) * s92levels, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c92_lvN, s92lvN, sizeof(int) * s92levels, 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c92_nLevels, &s92levels, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+  cudaMemcpyToSymbolAsync(c92_order, &s92n, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, cudaEvent_t u0,
+                         cudaEvent_t u1) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_unit_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  if (smemBytes > 200 * 1024) return 3;
+  launch_prologue(J, st);
+  long long nUnits = (long long)J.nCentres * J.nPairs;
+  if (u0) cudaEventRecord(u0, st);
+  if (nUnits > 0) k_unit_fast<<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(J);
+  if (u1) cudaEventRecord(u1, st);
+  launch_epilogue(J, st);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+}  // namespace ecpgb

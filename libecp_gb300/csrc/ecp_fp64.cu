@@ -24,192 +24,9 @@
 #include <climits>
 #include <cmath>
 
-#include "ecp_engine.h"
-#include "ecp_tables.h"
+#include "ecp_device.cuh"
 
 namespace ecpgb {
-
-#define NCART(l) (((l) + 1) * ((l) + 2) / 2)
-#define NCUM(l) (((l) + 1) * ((l) + 2) * ((l) + 3) / 6)
-
-static constexpr double kPi = 3.14159265358979323846;
-static constexpr int kMaxRows = 40;   // Bessel rows incl. the 5 Taylor guard rows
-
-__constant__ int c93_slot[kSmallOrder];
-__constant__ int c93_lvEnd[32], c93_lvJ[32], c93_lvN[32];
-__constant__ int c93_nLevels;
-__constant__ int c92_slot[kMaxLargeOrder];
-__constant__ int c92_lvEnd[32], c92_lvN[32];
-__constant__ int c92_nLevels, c92_order;
-
-// ------------------------------------------------------------ primitives
-
-// K_0..K_lmax(z) = exp(-z) i_l(z) with stride; three branches of
-// src/bessel.c:102-199 (small z, 5-term Taylor about the nearest table point,
-// asymptotic).  The table is stored transposed: row i holds K_0..K_tabL(z_i).
-__device__ void bessel_eval(const DevJob &J, int lmax, double z, double *K, int stride) {
-  if (z < 1.0E-7) {
-    if (z <= 0) {
-      K[0] = 1.0;
-      for (int l = 1; l <= lmax; l++) K[l * stride] = 0.0;
-    } else {
-      K[0] = 1 - z;
-      for (int l = 1; l <= lmax; l++) K[l * stride] = K[(l - 1) * stride] * z / (2 * l + 1);
-    }
-  } else if (z < 16.0) {
-    int top = lmax + 5;
-    double d[kMaxRows], prev[kMaxRows];
-    double h = J.besselN / 16;  // integer division, as the reference
-    int index = (int)floor(z * h + 0.5);
-    double dz = z - index / h, scale = 1.0;
-    const double *row = J.besT + (size_t)index * (J.tabL + 1);
-    for (int l = 0; l <= top; l++) d[l] = row[l];
-    for (int l = 0; l <= lmax; l++) K[l * stride] = d[l];
-    for (int i = 1; i <= 5; i++) {
-      int ti = top - i;
-      for (int j = 0; j <= ti + 1; j++) prev[j] = d[j];
-      d[0] = prev[1] - prev[0];
-      for (int j = 1; j <= ti; j++)
-        d[j] = J.besC[j] * (prev[j - 1] - prev[j + 1]) - prev[j] + prev[j + 1];
-      scale = scale * dz / i;
-      for (int j = 0; j <= lmax; j++) K[j * stride] += scale * d[j];
-    }
-  } else {
-    double A[kMaxRows];
-    A[0] = 0.5 / z;
-    for (int l = 0; l <= lmax; l++) K[l * stride] = A[0];
-    for (int l = 1; l <= lmax; l++) {
-      double f = l * (l + 1);
-      for (int i = 1; i < l; i++) {
-        K[l * stride] += f * A[i];
-        f *= (l + i + 1) * (l - i);
-      }
-      A[l] = -A[0] * A[l - 1] / l;
-      K[l * stride] += f * A[l];
-    }
-  }
-}
-
-// r^n for the ECP exponent n (a double in the interface; integers are the norm).
-__device__ inline double rpow(double r, double n) {
-  if (n == 0.0) return 1.0;
-  if (n == 1.0) return r;
-  if (n == 2.0) return r * r;
-  return pow(r, n);
-}
-
-// U_l(r) of centre c (src/ecp.c:42-60).
-__device__ double eval_ecp(const DevJob &J, int c, int l, double r) {
-  double pot = 0.0, r2 = r * r;
-  int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
-  for (int t = t0; t < t1; t++)
-    if (J.termL[t] == l) pot += rpow(r, J.termN[t]) * J.termD[t] * exp(-J.termA[t] * r2);
-  return pot;
-}
-
-// (r, theta, phi); src/util.c:75-106.
-__device__ void to_spherical(const double *v, double *out) {
-  const double eps = 1.0E-14;
-  double x = v[0], y = v[1], z = v[2];
-  double r = sqrt(x * x + y * y + z * z), th, ph;
-  th = (r < eps) ? 0.0 : acos(z / r);
-  if (fabs(x) < eps) {
-    if (fabs(y) < eps) ph = 0.0;
-    else if (y < 0.0) ph = 1.5 * kPi;
-    else ph = 0.5 * kPi;
-  } else {
-    ph = (x > 0.0) ? atan(y / x) : atan(y / x) + kPi;
-  }
-  out[0] = r; out[1] = th; out[2] = ph;
-}
-
-// Real spherical harmonics, index l*l + l + m (m = -l..l);
-// src/spherical_harmonics.c:16-114.  lmax <= 12.
-__device__ void real_sph(const DevJob &J, int lmax, double theta, double phi, double *rsh) {
-  double P[169], s[14], c[14];
-  int n = (lmax + 1) * (lmax + 1);
-  for (int i = 0; i < n; i++) P[i] = 0.0;
-  for (int i = 0; i < 14; i++) { s[i] = 0.0; c[i] = 0.0; }
-#define PL(l, m) P[(l) * (l) + (m) + (l)]
-  double x = cos(theta);
-  if (1.0 == x) {
-    for (int l = 0; l <= lmax; l++) PL(l, 0) = 1.0;
-  } else if (-1.0 == x) {
-    PL(0, 0) = 1.0;
-    for (int l = 1; l <= lmax; l++) PL(l, 0) = -PL(l - 1, 0);
-  } else {
-    s[1] = sqrt(1.0 - x * x);
-    for (int l = 2; l <= lmax; l++) s[l] = s[l - 1] * s[1];
-    for (int l = 0; l <= lmax; l++) {
-      if (l == 0) { PL(0, 0) = 1.0; continue; }
-      PL(l, l) = s[l] * J.dfac[2 * l - 1];
-      int m = l - 1;
-      PL(l, m) = x * (2 * m + 1) * PL(l - 1, m);
-      if (l > 1)
-        for (m = 0; m <= l - 2; m++)
-          PL(l, m) = (x * (2 * l - 1) * PL(l - 1, m) - (l + m - 1) * PL(l - 2, m)) / (l - m);
-    }
-  }
-  for (int l = 0; l <= lmax; l++) {
-    double norm0 = sqrt((2.0 * l + 1.0) / (2.0 * kPi));
-    PL(l, 0) = norm0 * PL(l, 0);
-    for (int m = 1; m <= l; m++) {
-      double norm = sqrt(J.fac[l - m] / J.fac[l + m]) * norm0;
-      PL(l, m) = norm * PL(l, m);
-    }
-  }
-  if (lmax > 0) {
-    if (0.0 == phi) {
-      for (int m = 0; m <= lmax; m++) { s[m] = 0.0; c[m] = 1.0; }
-    } else {
-      s[1] = sin(phi);
-      c[1] = cos(phi);
-      for (int m = 2; m <= lmax; m++) {
-        s[m] = s[1] * c[m - 1] + c[1] * s[m - 1];
-        c[m] = c[1] * c[m - 1] - s[1] * s[m - 1];
-      }
-    }
-  }
-  for (int l = 0; l <= lmax; l++) {
-    rsh[l * l + l] = PL(l, 0) / sqrt(2.0);
-    for (int m = 1; m <= l; m++) {
-      rsh[l * l + l - m] = PL(l, m) * s[m];
-      rsh[l * l + l + m] = PL(l, m) * c[m];
-    }
-  }
-#undef PL
-}
-
-// Squared radius where c r^l exp(-zeta r^2) = cutoff; -1 if Newton fails
-// (src/util.c:134-172, where the reference asserts).
-__device__ double gto_radius(double c, double zeta, int l, double cutoff) {
-  double delta, dg, guess, zr, r;
-  const double t = log(fabs(c) / fabs(cutoff));
-  dg = t / zeta;
-  r = (dg > cutoff) ? dg : cutoff;
-  if (l != 0) {
-    bool ok = false;
-    if (l > 0) {
-      dg = sqrt(0.5 * l / fabs(c));
-      guess = (dg > cutoff) ? dg : cutoff;
-      if (guess > r) r = 0.5 * (r + guess);
-    }
-    for (int i = 0; i < 40; i++) {
-      zr = zeta * r;
-      guess = t + l * log(r) - zr * r;
-      delta = guess / (l / r - 2 * zr);
-      dg = r - delta;
-      r = (dg > cutoff) ? dg : cutoff;
-      if (fabs(delta) < cutoff) { r *= r; ok = true; break; }
-    }
-    if (!ok) return -1.0;
-  }
-  return r;
-}
-
-__device__ inline double binom(const double *fac, int n, int k) {
-  return (k >= 0 && k <= n) ? fac[n] / (fac[n - k] * fac[k]) : 0.0;
-}
 
 // ------------------------------------------------------------- small kernels
 
@@ -350,55 +167,6 @@ __global__ void __launch_bounds__(128) k_shell_F(DevJob J) {
     }
     for (int i = 0; i < nF; i++) F[(size_t)n * nF + i] = acc[i];
   }
-}
-
-// ------------------------------------------------------------ quadratures
-
-// Adaptive PS93 walk over the small grid (src/gc_integrators.c:157-217):
-// `f(n)` is the integrand at abscissa index n; lower-half points count from
-// `start`, upper-half points up to `end`; a level that touches no point skips
-// the absolute error test.
-template <class Fn>
-__device__ bool ps93_walk(const double *w, int start, int end, double tol, Fn f, double &res) {
-  int mid = c93_slot[0], a = c93_slot[1], b = c93_slot[2];
-  double p = w[mid] * f(mid);
-  double q = w[a] * f(a) + w[b] * f(b);
-  double I = p + q, err = 0.0;
-  int pos = 3;
-  for (int k = 0; k < c93_nLevels; k++) {
-    int j = c93_lvJ[k], cnt = 0, e = c93_lvEnd[k];
-    for (; pos < e; pos += 2) {
-      int lo = c93_slot[pos], hi = c93_slot[pos + 1];
-      double T = 0.0;
-      if (lo >= start) { T += w[lo] * f(lo); cnt++; }
-      if (hi <= end) { T += w[hi] * f(hi); cnt++; }
-      I += T;
-    }
-    int n = c93_lvN[k];
-    p += (1 - j) * (I - q);
-    if (cnt > 0) err = 16 * fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q)) / (3 * n);
-    q = (1 - j) * q + j * I;
-    if (cnt == 0) continue;
-    if (err < tol) {
-      res = 16 * q / (3 * n);
-      return true;
-    }
-  }
-  return false;
-}
-
-// PSM92 walk state (src/gc_integrators.c:39-86) advanced chunk by chunk over
-// the schedule.  st = {I, p, q, result}; done = 1 converged.
-struct Walk {
-  double *I, *p, *q, *res;
-  int *done;
-};
-
-// Level of schedule slot pos (pos >= 1).
-__device__ inline int level_of(int pos) {
-  int k = 0;
-  while (c92_lvEnd[k] <= pos) k++;
-  return k;
 }
 
 // ------------------------------------------------------------ unit kernel
@@ -945,16 +713,25 @@ int launch_fp64_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, cud
     attr = true;
   }
   if (smemBytes > 200 * 1024) return 3;
-  k_radius<<<(J.nShells + 127) / 128, 128, 0, st>>>(J);
-  k_centre<<<J.nCentres, 128, sizeof(double) * kSmallOrder * (kMaxLEcp + 1), st>>>(J);
-  k_centre_atom<<<dim3(J.nAtoms, J.nCentres), 64, 0, st>>>(J);
-  k_shell_F<<<dim3(J.nShells, J.nCentres), 128, 0, st>>>(J);
+  launch_prologue(J, st);
   long long nUnits = (long long)J.nCentres * J.nPairs;
   if (u0) cudaEventRecord(u0, st);
   if (nUnits > 0) k_unit<<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(J);
   if (u1) cudaEventRecord(u1, st);
-  if (J.nPairs > 0) k_scatter<<<J.nPairs, 128, 0, st>>>(J);
+  launch_epilogue(J, st);
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Per-job stages before and after the unit kernel; shared by both paths.
+void launch_prologue(const DevJob &J, cudaStream_t st) {
+  k_radius<<<(J.nShells + 127) / 128, 128, 0, st>>>(J);
+  k_centre<<<J.nCentres, 128, sizeof(double) * kSmallOrder * (kMaxLEcp + 1), st>>>(J);
+  k_centre_atom<<<dim3(J.nAtoms, J.nCentres), 64, 0, st>>>(J);
+  k_shell_F<<<dim3(J.nShells, J.nCentres), 128, 0, st>>>(J);
+}
+
+void launch_epilogue(const DevJob &J, cudaStream_t st) {
+  if (J.nPairs > 0) k_scatter<<<J.nPairs, 128, 0, st>>>(J);
 }
 
 }  // namespace ecpgb

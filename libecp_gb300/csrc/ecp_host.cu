@@ -144,7 +144,7 @@ int parse_system(const ecpgb_system &s, Parsed &P) {
 struct DevTables {
   TableKey key{};
   HostTables host;
-  DBuf<double> xs, ws, xl, wl, besT, besC, p2s, fac, dfac, omega;
+  DBuf<double> xs, ws, xl, wl, besT, besC, besH, shNorm, p2s, fac, dfac, omega;
   DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items;
   int nItemsMax = 0;
 };
@@ -186,7 +186,8 @@ struct Engine {
               t->besC.upload(h.besselC, stream) && t->p2s.upload(h.poly2sph, stream) &&
               t->fac.upload(h.fac, stream) && t->dfac.upload(h.dfac, stream) &&
               t->omega.upload(h.omega, stream) && t->ijk.upload(h.ijk, stream) &&
-              t->ijkIdx.upload(h.ijkIndex, stream);
+              t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) &&
+              t->shNorm.upload(h.shNorm, stream);
     // used-triple lists per (la, lb, l)
     int LB = h.maxLBS, LE = h.maxLECP > 0 ? h.maxLECP : 1;
     std::vector<int> off, cnt, items, tmp;
@@ -224,6 +225,11 @@ struct Engine {
                               h.s93.lvJ.data(), h.s93.lvN.data(), h.s93.nLevels, h.s92.slot.data(),
                               (int)h.s92.slot.size(), h.s92.lvEnd.data(), h.s92.lvN.data(),
                               h.s92.nLevels, stream);
+    if (!rc)
+      rc = upload_schedules_fast(h.s93.slot.data(), (int)h.s93.slot.size(), h.s93.lvEnd.data(),
+                                 h.s93.lvJ.data(), h.s93.lvN.data(), h.s93.nLevels, h.s92.slot.data(),
+                                 (int)h.s92.slot.size(), h.s92.lvEnd.data(), h.s92.lvN.data(),
+                                 h.s92.nLevels, stream);
     if (rc) {
       set_error("schedule upload failed (%d)", rc);
       return -1;
@@ -319,18 +325,24 @@ static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers 
   J.radius = B.radius.p; J.utab = B.utab.p; J.uL = B.uL.p; J.gridEnd = B.gridEnd.p; J.win = B.win.p;
   J.F = B.F.p; J.cgeo = B.cgeo.p; J.usp = B.usp.p; J.ang = B.ang.p; J.out = B.out.p;
   J.status = B.status.p; J.mat = B.mat.p; J.errWord = B.err.p;
+  J.besH = T->besH.p;
+  J.besHL = h.besselHL;
+  J.shNorm = T->shNorm.p;
   UnitSmem L = unit_smem_layout(h.maxLBS, h.maxLECP, h.nF);
   B.smem = sizeof(double) * (size_t)L.total;
+  B.smemFast = fast_smem_bytes(h.maxLBS, h.maxLECP, h.nF);
   return 0;
 }
 
-// Resets the per-run outputs and launches the pipeline.
-static int run_pipeline(Engine &E, JobBuffers &B, const DevJob &J, cudaEvent_t u0, cudaEvent_t u1) {
+// Resets the per-run outputs and launches the pipeline of the mode.
+static int run_pipeline(Engine &E, JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0,
+                        cudaEvent_t u1) {
   int init[2] = {INT_MAX, 0};
   std::memcpy(B.pinnedErr, init, sizeof init);
   CUDA_OK(cudaMemcpyAsync(B.err.p, B.pinnedErr, sizeof init, cudaMemcpyHostToDevice, E.stream));
   CUDA_OK(cudaMemsetAsync(B.mat.p, 0, sizeof(double) * (size_t)J.dim * J.dim, E.stream));
-  int rc = launch_fp64_pipeline(J, E.stream, B.smem, u0, u1);
+  int rc = mode == ECPGB_FAST ? launch_fast_pipeline(J, E.stream, B.smemFast, u0, u1)
+                              : launch_fp64_pipeline(J, E.stream, B.smem, u0, u1);
   if (rc) {
     set_error("kernel launch failed (%d): %s", rc, cudaGetErrorString(cudaGetLastError()));
     return -1;
@@ -343,7 +355,7 @@ static int run_pipeline(Engine &E, JobBuffers &B, const DevJob &J, cudaEvent_t u
 int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_info *info) {
   Engine &E = engine();
   std::lock_guard<std::mutex> lk(E.mu);
-  if (mode != ECPGB_FP64) { set_error("unknown mode %d", mode); return 1; }
+  if (mode != ECPGB_FP64 && mode != ECPGB_FAST) { set_error("unknown mode %d", mode); return 1; }
   if (E.ensure_init()) return 1;
   Parsed P;
   if (parse_system(s, P)) return 1;
@@ -360,7 +372,7 @@ int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_inf
   cudaEvent_t e0, e1, u0, u1;
   cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
   cudaEventRecord(e0, E.stream);
-  if (run_pipeline(E, B, J, u0, u1)) return 1;
+  if (run_pipeline(E, B, J, mode, u0, u1)) return 1;
   cudaEventRecord(e1, E.stream);
   size_t mb = sizeof(double) * (size_t)P.dim * P.dim;
   if (!B.pinnedOut.ensure(mb)) { set_error("pinned allocation failed"); return 1; }
@@ -394,7 +406,7 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
                ecpgb_info *info, Parsed *parsedOut) {
   Engine &E = engine();
   std::lock_guard<std::mutex> lk(E.mu);
-  if (mode != ECPGB_FP64) { set_error("unknown mode %d", mode); return 1; }
+  if (mode != ECPGB_FP64 && mode != ECPGB_FAST) { set_error("unknown mode %d", mode); return 1; }
   if (E.ensure_init()) return 1;
   Parsed P;
   if (parse_system(s, P)) return 1;
@@ -414,7 +426,7 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
   cudaEvent_t e0, e1, u0, u1;
   cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
   cudaEventRecord(e0, E.stream);
-  if (run_pipeline(E, B, J, u0, u1)) return 1;
+  if (run_pipeline(E, B, J, mode, u0, u1)) return 1;
   cudaEventRecord(e1, E.stream);
   if (values) cudaMemcpyAsync(values, B.out.p, sizeof(double) * nv, cudaMemcpyDeviceToHost, E.stream);
   std::vector<int> st(nUnits);
@@ -463,14 +475,16 @@ struct ResidentJob {
   JobBuffers B;
   DevJob J;
   int launches = 6;
+  int mode = ECPGB_FP64;
 };
 
 void *job_create(const ecpgb_system &s, int mode) {
   Engine &E = engine();
   std::lock_guard<std::mutex> lk(E.mu);
-  if (mode != ECPGB_FP64) { set_error("unknown mode %d", mode); return nullptr; }
+  if (mode != ECPGB_FP64 && mode != ECPGB_FAST) { set_error("unknown mode %d", mode); return nullptr; }
   if (E.ensure_init()) return nullptr;
   auto *R = new ResidentJob();
+  R->mode = mode;
   if (parse_system(s, R->P)) { delete R; return nullptr; }
   if (R->P.nCentres == 0 || R->P.nPairs == 0) { set_error("job has no units"); delete R; return nullptr; }
   R->T = E.get_tables({R->P.maxLECP, R->P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
@@ -491,7 +505,7 @@ int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
   for (int r = 0; r < nRuns; r++) {
     if (flushL2) cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
     cudaEventRecord(ev[4 * r], E.stream);
-    if (run_pipeline(E, R->B, R->J, ev[4 * r + 2], ev[4 * r + 3])) return 1;
+    if (run_pipeline(E, R->B, R->J, R->mode, ev[4 * r + 2], ev[4 * r + 3])) return 1;
     cudaEventRecord(ev[4 * r + 1], E.stream);
   }
   cudaError_t ce = cudaStreamSynchronize(E.stream);

@@ -83,7 +83,7 @@ struct JobBuffers {
   DBuf<int> gridEnd, win, status, err;
   PinnedBuf pinned, pinnedOut;
   int *pinnedErr = nullptr;
-  size_t smem = 0;
+  size_t smem = 0, smemFast = 0;
   long long h2dBytes = 0;
   JobBuffers() { cudaMallocHost((void **)&pinnedErr, 4 * sizeof(int)); }
   ~JobBuffers() {

@@ -377,6 +377,37 @@ void build_tables(const TableKey &key, HostTables &t) {
   }
   if (t.maxLECP > 0) omega_table(t);
   else t.omega.assign(1, 0.0);
+  bessel_horner(t);
+  const int W = t.tmDim + 1;
+  t.shNorm.assign((size_t)W * W, 0.0);
+  for (int l = 0; l < W; l++) {
+    double norm0 = std::sqrt((2.0 * l + 1.0) / (2.0 * kPi));
+    t.shNorm[(size_t)l * W] = norm0;
+    for (int m = 1; m <= l; m++) t.shNorm[(size_t)l * W + m] = std::sqrt(t.fac[l - m] / t.fac[l + m]) * norm0;
+  }
+}
+
+// Taylor coefficients D^k K_l(z_i)/k!, k = 0..5, of every table point: the
+// k-th derivative rows follow from the (k-1)-th by the recurrence of
+// src/bessel.c:195-212; row l of the 5th derivative needs rows up to l+5.
+void bessel_horner(HostTables &t) {
+  const int W = t.tabL + 1, N = t.besselN + 1, HL = t.tabL - 5;
+  static const double invfact[6] = {1.0, 1.0, 0.5, 1.0 / 6.0, 1.0 / 24.0, 1.0 / 120.0};
+  t.besselHL = HL;
+  t.besselH.assign((size_t)N * (HL + 1) * 6, 0.0);
+  std::vector<double> d(W + 1), prev(W + 1);
+  for (int i = 0; i < N; i++) {
+    for (int l = 0; l < W; l++) d[l] = t.besselT[(size_t)i * W + l];
+    double *c = &t.besselH[(size_t)i * (HL + 1) * 6];
+    for (int l = 0; l <= HL; l++) c[l * 6] = d[l];
+    for (int k = 1; k <= 5; k++) {
+      int top = t.tabL - k;
+      for (int j = 0; j <= top + 1; j++) prev[j] = d[j];
+      d[0] = prev[1] - prev[0];
+      for (int j = 1; j <= top; j++) d[j] = t.besselC[j] * (prev[j - 1] - prev[j + 1]) - prev[j] + prev[j + 1];
+      for (int l = 0; l <= HL; l++) c[l * 6 + k] = d[l] * invfact[k];
+    }
+  }
 }
 
 void used_triples(int la, int lb, int l, std::vector<int> &out) {

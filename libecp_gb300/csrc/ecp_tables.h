@@ -65,6 +65,16 @@ struct HostTables {
   Schedule s93, s92;
   std::vector<double> besselT;   // transposed Bessel table [i][l], (N+1) x (tabL+1)
   std::vector<double> besselC;   // C[l] = l/(2l+1)
+  // Taylor coefficients of K_l about every table point, [i][l][k], k = 0..5:
+  // D^k K_l(z_i) / k!, the derivatives from the reference's recurrence
+  // (src/bessel.c:195-212), for l <= besselHL.  K_l(z_i + dz) is then one
+  // Horner pass of five multiply-adds per row.
+  std::vector<double> besselH;
+  int besselHL = 0;
+  // Normalisation of the real spherical harmonics, [l][m] for l, m <= tmDim:
+  // sqrt((2l+1)/(2 pi)) and sqrt((l-m)!/(l+m)!) times that, computed as
+  // src/spherical_harmonics.c:236-243 does.
+  std::vector<double> shNorm;
   std::vector<double> omega;     // [nsph(maxLECP)][nsph(maxLambda)][ncum(maxAlpha)]
   int omD1 = 0, omD2 = 0;
   int status = 0;                // 0 ok, 1 Bessel series did not converge, 3 sizes out of range
@@ -72,6 +82,7 @@ struct HostTables {
 
 // Builds every table for the key.  status != 0 reports a failure.
 void build_tables(const TableKey &key, HostTables &t);
+void bessel_horner(HostTables &t);
 
 // Used triples (l1, l2, l3) of the type-2 radial table for one (la, lb, l):
 // exactly those the angular linking of calcGamma (src/type2.c:583-623) reads.
