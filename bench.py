@@ -169,7 +169,8 @@ def ours(args, rank, world):
         dist.init_process_group("nccl")
     system = make_workload(args.workload, rank)
     peaks = eg.measure_peaks()
-    job = eg.Job(system)
+    mode = eg.ECPGB_FAST if args.mode == "batched" else eg.ECPGB_FP64
+    job = eg.Job(system, mode=mode)
     job.run(args.warmup, flush_l2=True)
     n_units, emitted = job.units()
     if world > 1:
@@ -191,15 +192,23 @@ def ours(args, rank, world):
     value = total_units / (t_step / 1e3)
     launches = job.launches_per_run() * args.steps
     job.close()
+    plain = None
+    if mode != eg.ECPGB_FP64 and args.compare_plain:
+        # the plain FP64 drop-in kernels on the same job, for the batched / plain ratio
+        pj = eg.Job(system, mode=eg.ECPGB_FP64)
+        pj.run(1, flush_l2=True)
+        pms, _ = pj.run(2, flush_l2=True)
+        pj.close()
+        plain = total_units / (float(np.mean(pms)) / 1e3)
 
-    # end to end through the drop-in getIntegrals with host buffers
-    rc, _, info = eg.get_integrals_info(system)
+    # end to end through the C ABI with host buffers (ecpgb_getIntegrals: the
+    # getIntegrals call with the path chosen; one packed H2D, one D2H per step)
+    rc, _, info = eg.get_integrals_info(system, mode=mode)
     h2d, d2h = info["h2dBytes"], info["d2hBytes"]
     e2e_t = []
     for i in range(args.warmup + args.steps):
-        I = np.zeros((system.dim, system.dim))
         t0 = time.perf_counter()
-        eg.get_integrals(system, I)
+        eg.get_integrals_info(system, mode=mode)
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             e2e_t.append(dt)
@@ -217,12 +226,13 @@ def ours(args, rank, world):
         f_unit = algorithmic_flops(st) / max(st["blocks"], 1)
         achieved = f_unit * emitted / (t_unit / 1e3) / 1e12
         peak = peaks["fp64_fma_tflops"]
+        kernel = "k_unit_fast" if mode != eg.ECPGB_FP64 else "k_unit"
         traffic = None
         prof = os.path.join(ROOT, "profiles", "roofline_inputs.txt")
         if os.path.exists(prof):
             with open(prof) as f:
-                per_unit = json.load(f).get("dram_bytes_per_emitted_unit")
-            if per_unit:  # ncu dram read+write of one k_unit launch, scaled to this launch
+                per_unit = json.load(f).get(kernel, {}).get("dram_bytes_per_emitted_unit")
+            if per_unit:  # ncu dram read+write of one unit-kernel launch, scaled to this launch
                 traffic = per_unit * emitted
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -230,11 +240,15 @@ def ours(args, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD if args.workload == "cluster" else WORKLOAD + " [first 8 centres]",
                        "units_per_rank": int(n_units),
-                       "emitted_units_per_rank": int(emitted), "precision": "fp64 (plain path)",
+                       "emitted_units_per_rank": int(emitted),
+                       "path": "batched FP64 (ECPGB_FAST)" if mode != eg.ECPGB_FP64 else "plain FP64 drop-in (ECPGB_FP64)",
+                       "plain_fp64_value": plain,
                        "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "api": "getIntegrals (host buffers)"},
-            "roofline": {"bound": "fp64", "kernel": "k_unit", "achieved": achieved,
+                    "d2h_bytes_per_step": int(d2h),
+                    "api": "ecpgb_getIntegrals (the getIntegrals call, host buffers, path = mode)"},
+            "roofline": {"bound": "fp64", "kernel": kernel,
+                         "achieved": achieved,
                          "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "traffic": traffic,
                          "peak_source": "FP64 FMA pipe measured live by ecpgb_measure_peaks",
@@ -281,6 +295,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="batched", choices=["batched", "fp64"],
+                    help="batched: the fast FP64 path; fp64: the plain drop-in kernels")
+    ap.add_argument("--compare-plain", type=int, default=1,
+                    help="also time the plain FP64 path (2 steps) for the ratio")
     ap.add_argument("--workload", default="cluster", choices=["cluster", "cluster8"],
                     help="cluster8: the first 8 centres only (small case for profiler captures)")
     args = ap.parse_args()

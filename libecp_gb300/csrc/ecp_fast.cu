@@ -66,15 +66,15 @@ static __device__ double bessel_row(const DevJob &J, int l, double z) {
   return fma(v, dz, q[0]);
 }
 
-// U_l(r) for l = 0..lmax of centre c in one pass over its terms
-// (src/ecp.c:42-60); channels above lmax are skipped.
-static __device__ void channels(const DevJob &J, int c, double r, int lmax, double *U, int stride) {
+// U_l(r) of centre c for the channels l set in mask, in one pass over its
+// terms (src/ecp.c:42-60); the other entries of U are left untouched.
+static __device__ void channels_masked(const DevJob &J, int c, double r, unsigned mask, double *U) {
   double r2 = r * r;
-  for (int l = 0; l <= lmax; l++) U[l * stride] = 0.0;
+  for (unsigned m = mask; m; m &= m - 1) U[__ffs(m) - 1] = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
   for (int t = t0; t < t1; t++) {
     int l = J.termL[t];
-    if (l <= lmax) U[l * stride] += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
+    if (mask >> l & 1u) U[l] += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
   }
 }
 
@@ -169,7 +169,7 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF) {
   for (int lab = 0; lab <= 2 * LB; lab++) {
     int g = t1_group(lab), lq = lab + 1;
     if (g * lq * lq > rq) rq = g * lq * lq;
-    if (g * (2 + 2 * lq) > tt) tt = g * (2 + 2 * lq);
+    if (g * (3 + 2 * lq) > tt) tt = g * (3 + 2 * lq);
   }
   int o = 0;
   s.chi = o; o += nc * nc;
@@ -187,7 +187,7 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF) {
   s.Fb = kSmallOrder * nF;
   int t2a = 2 * kSmallOrder * nF;
   // type 2 fallback: 32-slot table (w, base, vis, U[nE], R[nA], Ka[LBE], Kb[LBE]) + walker state
-  s.tab2Stride = 3 + nE + nA + 2 * LBE;
+  s.tab2Stride = (3 + nE + nA + 2 * LBE) | 1;  // odd: conflict-free lane strides
   s.w2Tab = 0;
   s.w2I = 32 * s.tab2Stride;
   s.w2P = s.w2I + kWalkCap;
@@ -210,6 +210,8 @@ struct FastShared {
   int failIdx[kWalkCap];
   unsigned failMask[64];
   int nFail, nThis, nextBase;
+  unsigned passMask;            // channels read by this pass's failed quadratures
+  int passL1, passL2, passL3;   // highest Ka, Kb and r^l rows they read
   int warn;
 };
 
@@ -264,7 +266,8 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
                                     const double *pcA, const double *pzB, const double *pcB,
                                     const double *gA, const double *gB, int ws, int we, int &warn) {
   const int lane = threadIdx.x & 31, lab = la + lb, lq = lab + 1, O = kSmallOrder;
-  const int OL = J.largeOrder, TSl = 2 + 2 * lq, RQ = lq * lq, nq = t1_items(lab);
+  // odd entry stride: lanes touching neighbouring entries hit distinct banks
+  const int OL = J.largeOrder, TSl = 3 + 2 * lq, RQ = lq * lq, nq = t1_items(lab);
   double *sc = W + L.w1Sc, *rsh = W + L.w1Rsh, *Q = W + L.w1Q, *H = W + L.w1H, *tab = W + L.w1Tab;
   const double dAC = gA[3], dBC = gB[3];
   const double *uL = J.uL + (size_t)c * O;
@@ -305,30 +308,30 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     for (int e = lane; e < (s1 - s0) * G; e += 32) {
       const int t = s0 + e / G, gg = e % G, kk = p0 + gg, n = c93_slot[t];
       double *ent = tab + e * TSl;
-      ent[0] = J.wSmall[n];
+      // slot entry: [2, 2+lq) K_l(s r), [2+lq, 2+2lq) w * C1 U_L e^(..) r^l
       if (n >= ws && n < we) {
         const double za = pzA[kk / Nb], zb = pzB[kk % Nb], s = sc[gg * 4];
         double r = J.xSmall[n], ex = ((-za - zb) * r + s) * r;
         ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
-        ent[1] = sc[gg * 4 + 3] * uL[n] * ex;
+        const double wB = J.wSmall[n] * (sc[gg * 4 + 3] * uL[n] * ex);
         bessel_fast(J, lab, s * r, ent + 2, 1);
-        double *R = ent + 2 + lq;
-        R[0] = 1.0;
-        for (int l = 1; l <= lab; l++) R[l] = r * R[l - 1];
+        double *WR = ent + 2 + lq, rl = 1.0;
+        for (int l = 0; l <= lab; l++) {
+          WR[l] = wB * rl;
+          rl = r * rl;
+        }
       } else {
-        for (int l = 1; l < TSl; l++) ent[l] = 0.0;
+        for (int l = 2; l < TSl; l++) ent[l] = 0.0;
       }
     }
     __syncwarp();
-    auto val = [&](int t) {
-      const double *e = tab + ((t - s0) * G + g) * TSl;
-      return e[0] * (e[1] * e[2 + lq + l1] * e[2 + l2]);
-    };
+    auto ent_of = [&](int t) { return tab + ((t - s0) * G + g) * TSl; };
     int t = s0;
     if (t == 0) {
       if (!done) {
-        p = val(0);
-        q = val(1) + val(2);
+        const double *e0 = ent_of(0), *e1 = ent_of(1), *e2 = ent_of(2);
+        p = e0[2 + lq + l1] * e0[2 + l2];
+        q = fma(e2[2 + lq + l1], e2[2 + l2], e1[2 + lq + l1] * e1[2 + l2]);
         I = p + q;
       }
       t = 3;
@@ -338,8 +341,8 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       if (t == lvStart) cnt = 0;
       int lo = c93_slot[t], hi = c93_slot[t + 1];
       double T = 0.0;
-      if (lo >= ws) { if (!done) T += val(t); cnt++; }
-      if (hi <= we) { if (!done) T += val(t + 1); cnt++; }
+      if (lo >= ws) { if (!done) { const double *e = ent_of(t); T = e[2 + lq + l1] * e[2 + l2]; } cnt++; }
+      if (hi <= we) { if (!done) { const double *e = ent_of(t + 1); T = fma(e[2 + lq + l1], e[2 + l2], T); } cnt++; }
       if (!done) I += T;
       t += 2;
       if (t == c93_lvEnd[k]) {
@@ -476,9 +479,9 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
                                int k, int Nb, int nf, int c, int Lc, int la, int lb, const double *pzA,
                                const double *pcA, const double *pzB, const double *pcB, double dAC,
                                double dBC, int ncls, int &warn) {
-  const int lane = threadIdx.x & 31, lab = la + lb, nA = 2 * J.maxLBS + 1;
+  const int lane = threadIdx.x & 31, nA = 2 * J.maxLBS + 1;
   const int LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE, OL = J.largeOrder;
-  const int TS = L.tab2Stride, laC = la + Lc - 1, lbC = lb + Lc - 1;
+  const int TS = L.tab2Stride;
   double *tab = W + L.w2Tab, *sI = W + L.w2I, *sP = W + L.w2P, *sQ = W + L.w2Q, *sR = W + L.w2R;
   double *part = W + L.w2Part;
   const double za = pzA[k / Nb], ca = pcA[k / Nb], zb = pzB[k % Nb], cb = pcB[k % Nb];
@@ -513,12 +516,16 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
         double r = i1j * J.xLarge[n] + i2j, d1 = dAC - r, d2 = dBC - r;
         double ex = -zaj * d1 * d1 - zbj * d2 * d2;
         if (ex >= J.lnAcc2) {
-          e[1] = Ck * fast_exp(ex);
-          channels(J, c, r, Lc - 1, U, 1);
-          bessel_fast(J, laC, 2.0 * zaj * dAC * r, Ka, 1);
-          bessel_fast(J, lbC, 2.0 * zbj * dBC * r, Kb, 1);
+          // Ka rows carry the weight and prefactor: w * Ck * e^(..) * K_l1
+          const double wB = e[0] * (Ck * fast_exp(ex));
+          e[1] = 1.0;
+          // only the channels and rows this pass's quadratures read
+          channels_masked(J, c, r, S.passMask, U);
+          bessel_fast(J, S.passL1, 2.0 * zaj * dAC * r, Ka, 1);
+          for (int l = 0; l <= S.passL1; l++) Ka[l] *= wB;
+          bessel_fast(J, S.passL2, 2.0 * zbj * dBC * r, Kb, 1);
           R[0] = 1.0;
-          for (int l = 1; l <= lab; l++) R[l] = r * R[l - 1];
+          for (int l = 1; l <= S.passL3; l++) R[l] = r * R[l - 1];
         }
       }
     }
@@ -534,7 +541,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
         const double *e = tab + (t - s0) * TS;
         if (e[1] == 0.0) return 0.0;
         const double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
-        return e[0] * (e[1] * U[l] * R[l3] * Ka[l1] * Kb[l2]);
+        return Ka[l1] * Kb[l2] * U[l] * R[l3];
       };
       auto vis = [&](int t) { return tab[(t - s0) * TS + 2] != 0.0; };
       double I = sI[q], p = sP[q], qv = sQ[q], res = 0;
@@ -716,10 +723,24 @@ __global__ void __launch_bounds__(kUnitThreads) k_unit_fast(DevJob J) {
     while (S.nextBase < nItems) {
       if (tid == 0) {
         int nf = 0, q = S.nextBase;
+        unsigned mask = 0;
+        int m1 = 0, m2 = 0, m3 = 0;
         for (; q < nItems && nf < kWalkCap; q++)
-          if (S.failMask[q >> 5] & (1u << (q & 31))) S.failIdx[nf++] = q;
+          if (S.failMask[q >> 5] & (1u << (q & 31))) {
+            S.failIdx[nf++] = q;
+            int l, l1, l2, l3;
+            item(q, l, l1, l2, l3);
+            mask |= 1u << l;
+            m1 = l1 > m1 ? l1 : m1;
+            m2 = l2 > m2 ? l2 : m2;
+            m3 = l3 > m3 ? l3 : m3;
+          }
         S.nThis = nf;
         S.nextBase = q;
+        S.passMask = mask;
+        S.passL1 = m1;
+        S.passL2 = m2;
+        S.passL3 = m3;
       }
       __syncthreads();
       const int nf = S.nThis;
