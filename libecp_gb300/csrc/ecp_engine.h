@@ -65,6 +65,7 @@ struct DevJob {
   const double *xSmall, *wSmall, *xLarge, *wLarge;
   const double *besT, *besC;
   const double *besH;          // Taylor coefficients [i][l <= besHL][6] (batched path)
+  const double *besA;          // large-argument polynomial [l][i], stride max(besHL + 1, 6)
   int besHL;
   const double *shNorm;        // spherical-harmonic normalisation [l][m], side tmDim + 1
   const double *p2s, *fac, *dfac;

@@ -27,24 +27,41 @@ constexpr int kWalkCap = 128;  // large-grid quadratures per warp and pass
 
 // --------------------------------------------------------------- helpers
 
-// K_0..K_lmax(z): the branches of src/bessel.c:102-199 with the Taylor branch
-// evaluated from the coefficient table.
+// K_0..K_lmax(z): the branches of src/bessel.c:102-199.  The Taylor branch
+// (z < 16) and the large-argument branch are both one Horner pass per row, in
+// dz over the row's Taylor coefficients or in -1/(2z) over the row's
+// large-argument polynomial, so that lanes on either branch run the same
+// instructions: row l is a polynomial of degree max(5, l) whose coefficients
+// above the branch's own degree are zero.
 static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *K, int stride) {
-  if (z < 1.0E-7 || z >= 16.0) {
+  if (z < 1.0E-7) {
     bessel_eval(J, lmax, z, K, stride);
     return;
   }
-  double h = J.besselN / 16;
-  int index = (int)floor(z * h + 0.5);
-  double dz = z - index / h;
-  const double *c = J.besH + (size_t)index * (J.besHL + 1) * 6;
+  const bool asy = z >= 16.0;
+  const int HL1 = J.besHL + 1;
+  double x, mult = 1.0;
+  const double *cf;
+  int cs;
+  if (asy) {
+    mult = 0.5 / z;
+    x = -mult;
+    cf = J.besA;
+    cs = HL1 < 6 ? 6 : HL1;
+  } else {
+    const double h = J.besselN / 16;  // integer division, as the reference
+    const int index = (int)floor(z * h + 0.5);
+    x = z - index / h;
+    cf = J.besH + (size_t)index * HL1 * 6;
+    cs = 6;
+  }
   for (int l = 0; l <= lmax; l++) {
-    const double *q = c + 6 * l;
-    double v = fma(q[5], dz, q[4]);
-    v = fma(v, dz, q[3]);
-    v = fma(v, dz, q[2]);
-    v = fma(v, dz, q[1]);
-    K[l * stride] = fma(v, dz, q[0]);
+    const double *q = cf + l * cs;
+    double v = 0.0;
+    for (int k = l; k > 5; k--) v = fma(v, x, asy ? q[k] : 0.0);
+#pragma unroll
+    for (int k = 5; k >= 0; k--) v = fma(v, x, q[k]);
+    K[l * stride] = v * mult;
   }
 }
 
@@ -147,7 +164,11 @@ __host__ __device__ inline int t1_items(int lab) {
 }
 __host__ __device__ inline int t1_group(int lab) {
   int g = 32 / t1_items(lab);
-  return g > 8 ? 8 : (g < 1 ? 1 : g);
+  g = g > 8 ? 8 : (g < 1 ? 1 : g);
+  // the group's step table (33 slots x g entries of 2 (lab+1) + 1 doubles)
+  // stays within 33 x 45 doubles, so that three CTAs fit on an SM
+  while (g > 1 && g * (2 * lab + 3) > 45) g--;
+  return g;
 }
 
 struct FastSmem {
@@ -169,7 +190,10 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF) {
   for (int lab = 0; lab <= 2 * LB; lab++) {
     int g = t1_group(lab), lq = lab + 1;
     if (g * lq * lq > rq) rq = g * lq * lq;
-    if (g * (3 + 2 * lq) > tt) tt = g * (3 + 2 * lq);
+    // small-grid steps: 33 slots x g entries of 2 lq + 1; fallback steps: 32
+    // slots of 2 lq + 3
+    if (33 * g * (1 + 2 * lq) > tt) tt = 33 * g * (1 + 2 * lq);
+    if (32 * (3 + 2 * lq) > tt) tt = 32 * (3 + 2 * lq);
   }
   int o = 0;
   s.chi = o; o += nc * nc;
@@ -177,11 +201,11 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF) {
   s.T = o; o += nE * LBE * LBE * nA;
   s.phase = o;
   s.w1Sc = 0;
-  s.w1Rsh = 32;
+  s.w1Rsh = 48;  // pair scalars: 6 per pair, up to 8 pairs
   s.w1Q = s.w1Rsh + rq;
   s.w1H = s.w1Q + rq;
   s.w1Tab = s.w1H + ncAB;
-  s.w1Stride = s.w1Tab + 33 * tt;
+  s.w1Stride = s.w1Tab + tt;
   int t1 = kWarps * s.w1Stride;
   s.Fa = 0;
   s.Fb = kSmallOrder * nF;
@@ -266,8 +290,8 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
                                     const double *pcA, const double *pzB, const double *pcB,
                                     const double *gA, const double *gB, int ws, int we, int &warn) {
   const int lane = threadIdx.x & 31, lab = la + lb, lq = lab + 1, O = kSmallOrder;
-  // odd entry stride: lanes touching neighbouring entries hit distinct banks
-  const int OL = J.largeOrder, TSl = 3 + 2 * lq, RQ = lq * lq, nq = t1_items(lab);
+  // odd entry strides: lanes touching neighbouring entries hit distinct banks
+  const int OL = J.largeOrder, TSs = 1 + 2 * lq, TSf = 3 + 2 * lq, RQ = lq * lq, nq = t1_items(lab);
   double *sc = W + L.w1Sc, *rsh = W + L.w1Rsh, *Q = W + L.w1Q, *H = W + L.w1H, *tab = W + L.w1Tab;
   const double dAC = gA[3], dBC = gB[3];
   const double *uL = J.uL + (size_t)c * O;
@@ -278,16 +302,17 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     double P[3], Sp[3];
     for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * gA[i] + zb * gB[i]);
     to_spherical(P, Sp);
-    sc[lane * 4 + 0] = Sp[0];
-    sc[lane * 4 + 1] = Sp[1];
-    sc[lane * 4 + 2] = Sp[2];
-    sc[lane * 4 + 3] = ca * cb * fast_exp(-za * dAC * dAC - zb * dBC * dBC);
+    sc[lane * 6 + 0] = Sp[0];
+    sc[lane * 6 + 1] = Sp[1];
+    sc[lane * 6 + 2] = Sp[2];
+    sc[lane * 6 + 3] = ca * cb * fast_exp(-za * dAC * dAC - zb * dBC * dBC);
+    sc[lane * 6 + 4] = -za - zb;
   }
   __syncwarp();
   // (2) S_lm of every pair, one (pair, m) column per lane
   if (lane < G * lq) {
     int g = lane / lq, m = lane % lq;
-    rsh_column(J, lab, m, sc[g * 4 + 1], sc[g * 4 + 2], rsh + g * RQ);
+    rsh_column(J, lab, m, sc[g * 6 + 1], sc[g * 6 + 2], rsh + g * RQ);
   }
   for (int e = lane; e < G * RQ; e += 32) Q[e] = 0.0;
   __syncwarp();
@@ -306,32 +331,32 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
   for (int s0 = 0; s0 < O;) {
     const int s1 = step_end93(s0) < O ? step_end93(s0) : O;
     for (int e = lane; e < (s1 - s0) * G; e += 32) {
-      const int t = s0 + e / G, gg = e % G, kk = p0 + gg, n = c93_slot[t];
-      double *ent = tab + e * TSl;
-      // slot entry: [2, 2+lq) K_l(s r), [2+lq, 2+2lq) w * C1 U_L e^(..) r^l
+      const int t = s0 + e / G, gg = e % G, n = c93_slot[t];
+      double *ent = tab + e * TSs;
+      // slot entry: [0, lq) K_l(s r), [lq, 2lq) w * C1 U_L e^(..) r^l
       if (n >= ws && n < we) {
-        const double za = pzA[kk / Nb], zb = pzB[kk % Nb], s = sc[gg * 4];
-        double r = J.xSmall[n], ex = ((-za - zb) * r + s) * r;
+        const double s = sc[gg * 6];
+        double r = J.xSmall[n], ex = (sc[gg * 6 + 4] * r + s) * r;
         ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
-        const double wB = J.wSmall[n] * (sc[gg * 4 + 3] * uL[n] * ex);
-        bessel_fast(J, lab, s * r, ent + 2, 1);
-        double *WR = ent + 2 + lq, rl = 1.0;
+        const double wB = J.wSmall[n] * (sc[gg * 6 + 3] * uL[n] * ex);
+        bessel_fast(J, lab, s * r, ent, 1);
+        double *WR = ent + lq, rl = 1.0;
         for (int l = 0; l <= lab; l++) {
           WR[l] = wB * rl;
           rl = r * rl;
         }
       } else {
-        for (int l = 2; l < TSl; l++) ent[l] = 0.0;
+        for (int l = 0; l < 2 * lq; l++) ent[l] = 0.0;
       }
     }
     __syncwarp();
-    auto ent_of = [&](int t) { return tab + ((t - s0) * G + g) * TSl; };
+    auto ent_of = [&](int t) { return tab + ((t - s0) * G + g) * TSs; };
     int t = s0;
     if (t == 0) {
       if (!done) {
         const double *e0 = ent_of(0), *e1 = ent_of(1), *e2 = ent_of(2);
-        p = e0[2 + lq + l1] * e0[2 + l2];
-        q = fma(e2[2 + lq + l1], e2[2 + l2], e1[2 + lq + l1] * e1[2 + l2]);
+        p = e0[lq + l1] * e0[l2];
+        q = fma(e2[lq + l1], e2[l2], e1[lq + l1] * e1[l2]);
         I = p + q;
       }
       t = 3;
@@ -341,8 +366,8 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       if (t == lvStart) cnt = 0;
       int lo = c93_slot[t], hi = c93_slot[t + 1];
       double T = 0.0;
-      if (lo >= ws) { if (!done) { const double *e = ent_of(t); T = e[2 + lq + l1] * e[2 + l2]; } cnt++; }
-      if (hi <= we) { if (!done) { const double *e = ent_of(t + 1); T = fma(e[2 + lq + l1], e[2 + l2], T); } cnt++; }
+      if (lo >= ws) { if (!done) { const double *e = ent_of(t); T = e[lq + l1] * e[l2]; } cnt++; }
+      if (hi <= we) { if (!done) { const double *e = ent_of(t + 1); T = fma(e[lq + l1], e[l2], T); } cnt++; }
       if (!done) I += T;
       t += 2;
       if (t == c93_lvEnd[k]) {
@@ -371,7 +396,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     if (!__ballot_sync(0xffffffffu, fail)) continue;
     const int kk = p0 + gg;
     const double za = pzA[kk / Nb], ca = pcA[kk / Nb], zb = pzB[kk % Nb], cb = pcB[kk % Nb];
-    const double s = sc[gg * 4], z = -za - zb, zd2 = -za * dAC * dAC - zb * dBC * dBC;
+    const double s = sc[gg * 6], z = -za - zb, zd2 = -za * dAC * dAC - zb * dBC * dBC;
     const double C2 = ca * cb;
     double i1, i2;
     fm06(za, zb, dAC, dBC, i1, i2);
@@ -394,7 +419,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       for (int t = s0 + lane; t < s1; t += 32) {
         int n = c92_slot[t];
         bool upper = t > 0 && ((t - 1) & 1);
-        double *e = tab + (t - s0) * TSl;
+        double *e = tab + (t - s0) * TSf;
         double *K = e + 2, *R = e + 2 + lq;
         e[0] = J.wLarge[n] * i1;
         e[1] = 0.0;
@@ -428,7 +453,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       __syncwarp();
       if (!done2) {
         auto val = [&](int t) {
-          const double *e = tab + (t - s0) * TSl;
+          const double *e = tab + (t - s0) * TSf;
           return e[1] == 0.0 ? 0.0 : e[0] * (e[1] * e[2 + lq + l1] * e[2 + l2]);
         };
         auto vis = [&](int t) { return c92_slot[t] <= end; };
@@ -823,10 +848,17 @@ int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, con
 
 int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, cudaEvent_t u0,
                          cudaEvent_t u1) {
-  static bool attr = false;
-  if (!attr) {
+  // function attributes are per device; callers hold the engine lock
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
     cudaFuncSetAttribute(k_unit_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
+    // the whole unified L1/shared array as shared memory: three CTAs of
+    // <= 72 KB per SM
+    cudaFuncSetAttribute(k_unit_fast, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    attr[dev] = true;
   }
   if (smemBytes > 200 * 1024) return 3;
   launch_prologue(J, st);

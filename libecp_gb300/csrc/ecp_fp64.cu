@@ -707,10 +707,13 @@ int upload_schedules(const int *s93slot, int s93n, const int *s93lvEnd, const in
 
 int launch_fp64_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, cudaEvent_t u0,
                          cudaEvent_t u1) {
-  static bool attr = false;
-  if (!attr) {
+  // function attributes are per device; callers hold the engine lock
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
     cudaFuncSetAttribute(k_unit, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
+    attr[dev] = true;
   }
   if (smemBytes > 200 * 1024) return 3;
   launch_prologue(J, st);

@@ -144,7 +144,7 @@ int parse_system(const ecpgb_system &s, Parsed &P) {
 struct DevTables {
   TableKey key{};
   HostTables host;
-  DBuf<double> xs, ws, xl, wl, besT, besC, besH, shNorm, p2s, fac, dfac, omega;
+  DBuf<double> xs, ws, xl, wl, besT, besC, besH, besA, shNorm, p2s, fac, dfac, omega;
   DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items;
   int nItemsMax = 0;
 };
@@ -186,7 +186,7 @@ struct Engine {
               t->besC.upload(h.besselC, stream) && t->p2s.upload(h.poly2sph, stream) &&
               t->fac.upload(h.fac, stream) && t->dfac.upload(h.dfac, stream) &&
               t->omega.upload(h.omega, stream) && t->ijk.upload(h.ijk, stream) &&
-              t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) &&
+              t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) && t->besA.upload(h.besselA, stream) &&
               t->shNorm.upload(h.shNorm, stream);
     // used-triple lists per (la, lb, l)
     int LB = h.maxLBS, LE = h.maxLECP > 0 ? h.maxLECP : 1;
@@ -326,6 +326,7 @@ static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers 
   J.F = B.F.p; J.cgeo = B.cgeo.p; J.usp = B.usp.p; J.ang = B.ang.p; J.out = B.out.p;
   J.status = B.status.p; J.mat = B.mat.p; J.errWord = B.err.p;
   J.besH = T->besH.p;
+  J.besA = T->besA.p;
   J.besHL = h.besselHL;
   J.shNorm = T->shNorm.p;
   UnitSmem L = unit_smem_layout(h.maxLBS, h.maxLECP, h.nF);

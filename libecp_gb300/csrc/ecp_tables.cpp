@@ -408,6 +408,17 @@ void bessel_horner(HostTables &t) {
       for (int l = 0; l <= HL; l++) c[l * 6 + k] = d[l] * invfact[k];
     }
   }
+  const int AS = HL + 1 < 6 ? 6 : HL + 1;
+  t.besselA.assign((size_t)(HL + 1) * AS, 0.0);
+  for (int l = 0; l <= HL; l++) {
+    double f = l * (l + 1.0), ifac = 1.0;
+    t.besselA[(size_t)l * AS] = 1.0;
+    for (int i = 1; i <= l; i++) {
+      ifac *= i;
+      t.besselA[(size_t)l * AS + i] = f / ifac;
+      f *= (double)(l + i + 1) * (l - i);
+    }
+  }
 }
 
 void used_triples(int la, int lb, int l, std::vector<int> &out) {

@@ -71,6 +71,11 @@ struct HostTables {
   // Horner pass of five multiply-adds per row.
   std::vector<double> besselH;
   int besselHL = 0;
+  // The large-argument branch (z >= 16, src/bessel.c:170-190) as a polynomial:
+  // K_l(z) = a * sum_i besselA[l][i] (-a)^i with a = 1/(2z), i <= l, row stride
+  // max(besselHL + 1, 6), zero beyond i = l.  The coefficients are the integers (l+i)!/((l-i)! i!), the
+  // reference's running product divided by i!, so they are exact in FP64.
+  std::vector<double> besselA;
   // Normalisation of the real spherical harmonics, [l][m] for l, m <= tmDim:
   // sqrt((2l+1)/(2 pi)) and sqrt((l-m)!/(l+m)!) times that, computed as
   // src/spherical_harmonics.c:236-243 does.
