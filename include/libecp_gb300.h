@@ -91,6 +91,38 @@ long long ecpgb_job_units(const ecpgb_job *j, long long *emitted);
 int ecpgb_job_kernel_launches(const ecpgb_job *j);           /* kernels per run */
 void ecpgb_job_free(ecpgb_job *j);
 
+/* Launch configuration of the batched path (ECPGB_FAST).  queue: 1 = a
+ * persistent launch whose CTAs pull units from a work queue, 0 = one CTA per
+ * unit; sorted: 1 = the queue holds the units by descending estimated cost
+ * (primitive pairs x (la + lb + 2) x (L + 2)), 0 = the reference's order;
+ * gcap: width cap of the type-1 step table in doubles per slot, which sets
+ * the primitive pairs per warp and the CTAs per SM.  msUnit: the unit
+ * kernel's time when the autotuner measured it, else 0. */
+typedef struct {
+  int queue, sorted, gcap;
+  float msUnit;
+} ecpgb_launch_config;
+
+/* Autotuner: times each candidate configuration on the job (one untimed and
+ * two timed runs each, unit kernel only), keeps the fastest for this job and
+ * for later jobs of the same (max basis l, max ECP L) in this process, and
+ * reports it in *chosen.  trials (may be NULL) receives up to maxTrials
+ * candidates with their times; *nTrials the number written.  queue and sorted
+ * leave every result bit for bit unchanged; gcap regroups the primitive pairs
+ * of the type-1 sums over warps, which moves results at rounding level only.
+ * 0 ok, 1 error, 3 the job is not a batched-path job. */
+int ecpgb_job_tune(ecpgb_job *j, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials,
+                   int *nTrials);
+/* Sets (cfg != NULL) and/or reads (out != NULL) the job's configuration. */
+int ecpgb_job_config(ecpgb_job *j, const ecpgb_launch_config *cfg, ecpgb_launch_config *out);
+/* 1: ecpgb_job_run replays the pipeline as one captured CUDA graph (the
+ * default); 0: plain stream launches. */
+int ecpgb_job_use_graph(ecpgb_job *j, int on);
+/* The last run's unit values (layout of ecpgb_blocks: unit u's blocks at
+ * offset (u / nPairs) * centre stride + the pair's offset) and unit statuses;
+ * either pointer may be NULL. */
+int ecpgb_job_blocks(ecpgb_job *j, double *values, int *status);
+
 /* Pipe-throughput probe on the current device: out[0] FP64 FMA TFLOP/s,
  * out[1] FP32 FMA TFLOP/s, out[2] MUFU ex2 Gop/s, out[3] FP64 exp() Gop/s.
  * Takes about 0.5 s.  0 ok. */

@@ -45,6 +45,14 @@ class EcpgbInfo(ct.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class LaunchConfig(ct.Structure):
+    """ecpgb_launch_config: batched-path launch configuration."""
+    _fields_ = [("queue", ct.c_int), ("sorted", ct.c_int), ("gcap", ct.c_int), ("msUnit", ct.c_float)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 ECP_CALLBACK = ct.CFUNCTYPE(None, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
                             ct.c_int, ct.c_int, ct.c_int, _D, ct.c_void_p)
 
@@ -84,6 +92,15 @@ def lib() -> ct.CDLL:
     L.ecpgb_job_units.restype = ct.c_longlong
     L.ecpgb_job_kernel_launches.argtypes = [ct.c_void_p]
     L.ecpgb_job_free.argtypes = [ct.c_void_p]
+    L.ecpgb_job_tune.argtypes = [ct.c_void_p, ct.POINTER(LaunchConfig), ct.POINTER(LaunchConfig), ct.c_int,
+                                 ct.POINTER(ct.c_int)]
+    L.ecpgb_job_tune.restype = ct.c_int
+    L.ecpgb_job_config.argtypes = [ct.c_void_p, ct.POINTER(LaunchConfig), ct.POINTER(LaunchConfig)]
+    L.ecpgb_job_config.restype = ct.c_int
+    L.ecpgb_job_use_graph.argtypes = [ct.c_void_p, ct.c_int]
+    L.ecpgb_job_use_graph.restype = ct.c_int
+    L.ecpgb_job_blocks.argtypes = [ct.c_void_p, _D, _I]
+    L.ecpgb_job_blocks.restype = ct.c_int
     L.ecpgb_job_free.restype = None
     L.ecpgb_measure_peaks.argtypes = [_D]
     L.ecpgb_last_error.restype = ct.c_char_p
@@ -250,6 +267,47 @@ class Job:
 
     def launches_per_run(self) -> int:
         return lib().ecpgb_job_kernel_launches(self._h)
+
+    def tune(self):
+        """Runs the autotuner; returns (chosen, trials) as dicts."""
+        chosen = LaunchConfig()
+        trials = (LaunchConfig * 16)()
+        n = ct.c_int(0)
+        rc = lib().ecpgb_job_tune(self._h, ct.byref(chosen), trials, 16, ct.byref(n))
+        if rc:
+            raise RuntimeError(f"ecpgb_job_tune failed ({rc}): {last_error()}")
+        return chosen.as_dict(), [trials[i].as_dict() for i in range(n.value)]
+
+    def config(self, queue=None, sorted=None, gcap=None) -> dict:
+        """Reads the launch configuration; sets the fields given."""
+        cur = LaunchConfig()
+        if lib().ecpgb_job_config(self._h, None, ct.byref(cur)):
+            raise RuntimeError(last_error())
+        if queue is None and sorted is None and gcap is None:
+            return cur.as_dict()
+        new = LaunchConfig(cur.queue if queue is None else int(queue),
+                           cur.sorted if sorted is None else int(sorted),
+                           cur.gcap if gcap is None else int(gcap), 0.0)
+        if lib().ecpgb_job_config(self._h, ct.byref(new), ct.byref(cur)):
+            raise RuntimeError(last_error())
+        return cur.as_dict()
+
+    def use_graph(self, on: bool = True) -> None:
+        if lib().ecpgb_job_use_graph(self._h, int(on)):
+            raise RuntimeError(last_error())
+
+    def blocks(self):
+        """Raw unit values (units' blocks at the ecpgb_blocks offsets) and the
+        per-unit status of the last run."""
+        cs = c_system(self.system)
+        nu, nv = ct.c_longlong(0), ct.c_longlong(0)
+        if lib().ecpgb_layout(ct.byref(cs), ct.byref(nu), ct.byref(nv)):
+            raise RuntimeError(last_error())
+        vals = np.zeros(max(nv.value, 1))
+        st = np.zeros(max(nu.value, 1), dtype=np.int32)
+        if lib().ecpgb_job_blocks(self._h, vals.ctypes.data_as(_D), st.ctypes.data_as(_I)):
+            raise RuntimeError(last_error())
+        return vals[:nv.value], st[:nu.value]
 
     def close(self):
         if self._h:

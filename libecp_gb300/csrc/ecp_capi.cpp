@@ -210,6 +210,21 @@ long long ecpgb_job_units(const ecpgb_job *j, long long *emitted) {
 
 int ecpgb_job_kernel_launches(const ecpgb_job *j) { return j ? ecpgb::job_launches(j->impl) : 0; }
 
+int ecpgb_job_tune(ecpgb_job *j, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials,
+                   int *nTrials) {
+  return j ? ecpgb::job_tune(j->impl, chosen, trials, maxTrials, nTrials) : 1;
+}
+
+int ecpgb_job_config(ecpgb_job *j, const ecpgb_launch_config *cfg, ecpgb_launch_config *out) {
+  return j ? ecpgb::job_config(j->impl, cfg, out) : 1;
+}
+
+int ecpgb_job_use_graph(ecpgb_job *j, int on) { return j ? ecpgb::job_use_graph(j->impl, on) : 1; }
+
+int ecpgb_job_blocks(ecpgb_job *j, double *values, int *status) {
+  return j ? ecpgb::job_blocks(j->impl, values, status) : 1;
+}
+
 void ecpgb_job_free(ecpgb_job *j) {
   if (!j) return;
   ecpgb::job_free(j->impl);

@@ -83,6 +83,17 @@ struct DevJob {
   int *status;
   double *mat;
   int *errWord;          // [0] first unit with a warning (atomicMin), [1] input error flags
+  // batched path: work queue and tuning
+  const int *order;              // units by descending estimated cost (null: natural order)
+  unsigned long long *queueHead; // next queue position (persistent launch); reset per run
+  int gcap;                      // type-1 step-table width cap (doubles per slot per warp)
+};
+
+// Launch configuration of the batched path (picked by the autotuner).
+struct FastConfig {
+  int queue = 1;   // 1: persistent CTAs pulling units from the work queue; 0: a CTA per unit
+  int sorted = 1;  // 1: units by descending estimated cost; 0: the reference's order
+  int gcap = 45;   // type-1 step-table width cap; smaller caps fit more CTAs per SM
 };
 
 // Shared-memory layout of the unit kernel (offsets in doubles).
@@ -128,6 +139,19 @@ __host__ __device__ inline UnitSmem unit_smem_layout(int LB, int LE, int nF) {
   return s;
 }
 
+// Records a timing event; under stream capture as an event-record node of
+// the graph (a plain record there only orders the capture).
+inline void record_timing(cudaEvent_t e, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cs);
+  if (cs == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+  else cudaEventRecord(e, st);
+}
+
+// Launchers return 0, 3 when the shared memory does not fit, or
+// kLaunchErrorBase + the cudaError_t of a failed launch.
+constexpr int kLaunchErrorBase = 1000;
+
 // Host-side launchers (ecp_fp64.cu).
 int upload_schedules(const int *s93slot, int s93n, const int *s93lvEnd, const int *s93lvJ,
                      const int *s93lvN, int s93levels, const int *s92slot, int s92n,
@@ -148,8 +172,15 @@ void launch_epilogue(const DevJob &job, cudaStream_t stream);
 int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, const int *s93lvJ,
                           const int *s93lvN, int s93levels, const int *s92slot, int s92n,
                           const int *s92lvEnd, const int *s92lvN, int s92levels, void *stream);
-size_t fast_smem_bytes(int LB, int LE, int nF);
-int launch_fast_pipeline(const DevJob &job, cudaStream_t stream, size_t smemBytes, cudaEvent_t u0,
-                         cudaEvent_t u1);
+size_t fast_smem_bytes(int LB, int LE, int nF, int gcap);
+// CTAs of the batched unit kernel resident per SM at smemBytes.
+int fast_ctas_per_sm(size_t smemBytes, int queue);
+// Sets the batched kernels' function attributes on the current device (call
+// before any graph capture).
+void fast_prepare();
+// Resets the per-run words (warning word, queue head).
+void launch_reset(const DevJob &job, cudaStream_t stream);
+int launch_fast_pipeline(const DevJob &job, cudaStream_t stream, size_t smemBytes, const FastConfig &cfg,
+                         cudaEvent_t u0, cudaEvent_t u1);
 
 }  // namespace ecpgb

@@ -162,12 +162,12 @@ __host__ __device__ inline int t1_items(int lab) {
   for (int l1 = 0; l1 <= lab; l1++) n += l1 / 2 + 1;
   return n;
 }
-__host__ __device__ inline int t1_group(int lab) {
+__host__ __device__ inline int t1_group(int lab, int cap) {
   int g = 32 / t1_items(lab);
   g = g > 8 ? 8 : (g < 1 ? 1 : g);
   // the group's step table (33 slots x g entries of 2 (lab+1) + 1 doubles)
-  // stays within 33 x 45 doubles, so that three CTAs fit on an SM
-  while (g > 1 && g * (2 * lab + 3) > 45) g--;
+  // stays within 33 x cap doubles (cap 45: three CTAs per SM at l <= 3, L <= 4)
+  while (g > 1 && g * (2 * lab + 3) > cap) g--;
   return g;
 }
 
@@ -181,14 +181,14 @@ struct FastSmem {
   int w2Stride, w2Tab, w2I, w2P, w2Q, w2R, w2Part, tab2Stride;
 };
 
-__host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF) {
+__host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap) {
   FastSmem s{};
   const int nA = 2 * LB + 1, nE = LE > 0 ? LE : 1, LBE = LB + nE;
   const int nc = (LB + 1) * (LB + 2) * (LB + 3) / 6, nct = (LB + 1) * (LB + 2) / 2;
   const int ncAB = (2 * LB + 1) * (2 * LB + 2) * (2 * LB + 3) / 6;
   int rq = 0, tt = 0;  // largest per-warp S_lm/Q and step-table widths over lab <= 2 LB
   for (int lab = 0; lab <= 2 * LB; lab++) {
-    int g = t1_group(lab), lq = lab + 1;
+    int g = t1_group(lab, cap), lq = lab + 1;
     if (g * lq * lq > rq) rq = g * lq * lq;
     // small-grid steps: 33 slots x g entries of 2 lq + 1; fallback steps: 32
     // slots of 2 lq + 3
@@ -227,7 +227,9 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF) {
   return s;
 }
 
-size_t fast_smem_bytes(int LB, int LE, int nF) { return sizeof(double) * (size_t)fast_layout(LB, LE, nF).total; }
+size_t fast_smem_bytes(int LB, int LE, int nF, int cap) {
+  return sizeof(double) * (size_t)fast_layout(LB, LE, nF, cap).total;
+}
 
 struct FastShared {
   int ppBreak[kMaxContraction * kMaxContraction];
@@ -590,10 +592,9 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
 
 // --------------------------------------------------------------- the kernel
 
-__global__ void __launch_bounds__(kUnitThreads) k_unit_fast(DevJob J) {
-  extern __shared__ double sm[];
-  __shared__ FastShared S;
-  const long long u = blockIdx.x;
+// One unit (centre c, shell pair pr) by the whole CTA.  Every thread enters
+// and leaves together (the early exits are CTA-uniform).
+static __device__ void unit_fast(const DevJob &J, const long long u, FastShared &S, double *sm) {
   const int c = (int)(u / J.nPairs), pr = (int)(u % J.nPairs);
   const int sa = J.pairA[pr], sb = J.pairB[pr], tid = threadIdx.x, NT = blockDim.x;
   const int warp = tid >> 5;
@@ -609,7 +610,7 @@ __global__ void __launch_bounds__(kUnitThreads) k_unit_fast(DevJob J) {
     if (tid == 0) J.status[u] = kUnitSkipped;
     return;
   }
-  const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.nF);
+  const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.nF, J.gcap);
   const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa], lb = J.shL[sb], lab = la + lb;
   const int nA = 2 * J.maxLBS + 1, LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE;
   const int Lc = J.ctrL[c], nca = NCUM(la), ncb = NCUM(lb), O = kSmallOrder;
@@ -631,7 +632,7 @@ __global__ void __launch_bounds__(kUnitThreads) k_unit_fast(DevJob J) {
     const int ncab = (lab + 1) * (lab + 2) * (lab + 3) / 6;
     for (int e = tid & 31; e < ncab; e += 32) W[Lm.w1H + e] = 0.0;
     __syncwarp();
-    const int G = t1_group(lab);
+    const int G = t1_group(lab, J.gcap);
     for (int p0 = warp * G; p0 < NP; p0 += kWarps * G)
       t1_group_run(J, Lm, W, c, Lc, la, lb, p0, NP - p0 < G ? NP - p0 : G, Nb, pzA, pcA, pzB, pcB, gA, gB,
                    ws, we, warn1);
@@ -825,6 +826,38 @@ __global__ void __launch_bounds__(kUnitThreads) k_unit_fast(DevJob J) {
   }
 }
 
+// A CTA per unit; blockIdx.x is a queue position.
+__global__ void __launch_bounds__(kUnitThreads) k_unit_fast(DevJob J) {
+  extern __shared__ double sm[];
+  __shared__ FastShared S;
+  const long long i = blockIdx.x;
+  unit_fast(J, J.order ? (long long)J.order[i] : i, S, sm);
+}
+
+// Persistent CTAs (as many as fit on the GPU) pulling queue positions from
+// one counter: the costliest units start first and the cheap ones fill the
+// tail, whatever order the hardware would dispatch CTAs in.
+__global__ void __launch_bounds__(kUnitThreads) k_unit_queue(DevJob J) {
+  extern __shared__ double sm[];
+  __shared__ FastShared S;
+  __shared__ long long next;
+  const long long n = (long long)J.nCentres * J.nPairs;
+  for (;;) {
+    if (threadIdx.x == 0) next = (long long)atomicAdd(J.queueHead, 1ull);
+    __syncthreads();
+    const long long i = next;
+    if (i >= n) break;
+    unit_fast(J, J.order ? (long long)J.order[i] : i, S, sm);
+    __syncthreads();  // shared state is rewritten by the next unit
+  }
+}
+
+__global__ void k_reset(int *errWord, unsigned long long *queueHead) {
+  errWord[0] = INT_MAX;
+  errWord[1] = 0;
+  if (queueHead) *queueHead = 0ull;
+}
+
 // --------------------------------------------------------------- launchers
 
 int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, const int *s93lvJ,
@@ -846,28 +879,59 @@ int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, con
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
-int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, cudaEvent_t u0,
-                         cudaEvent_t u1) {
+void fast_prepare() {
   // function attributes are per device; callers hold the engine lock
   static bool attr[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !attr[dev]) {
-    cudaFuncSetAttribute(k_unit_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (dev < 0 || dev >= 64 || attr[dev]) return;
+  for (const void *k : {(const void *)k_unit_fast, (const void *)k_unit_queue}) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     // the whole unified L1/shared array as shared memory: three CTAs of
     // <= 72 KB per SM
-    cudaFuncSetAttribute(k_unit_fast, cudaFuncAttributePreferredSharedMemoryCarveout,
-                         cudaSharedmemCarveoutMaxShared);
-    attr[dev] = true;
+    cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   }
+  attr[dev] = true;
+}
+
+int fast_ctas_per_sm(size_t smemBytes, int queue) {
+  fast_prepare();
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, queue ? (const void *)k_unit_queue : (const void *)k_unit_fast,
+                                                    kUnitThreads, smemBytes) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+void launch_reset(const DevJob &J, cudaStream_t st) { k_reset<<<1, 1, 0, st>>>(J.errWord, J.queueHead); }
+
+int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, const FastConfig &cfg,
+                         cudaEvent_t u0, cudaEvent_t u1) {
+  fast_prepare();
   if (smemBytes > 200 * 1024) return 3;
-  launch_prologue(J, st);
+  DevJob Jc = J;
+  Jc.gcap = cfg.gcap;
+  if (!cfg.sorted) Jc.order = nullptr;
+  launch_prologue(Jc, st);
   long long nUnits = (long long)J.nCentres * J.nPairs;
-  if (u0) cudaEventRecord(u0, st);
-  if (nUnits > 0) k_unit_fast<<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(J);
-  if (u1) cudaEventRecord(u1, st);
-  launch_epilogue(J, st);
-  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+  if (u0) record_timing(u0, st);
+  if (nUnits > 0) {
+    if (cfg.queue && J.queueHead) {
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      int per = fast_ctas_per_sm(smemBytes, 1);
+      long long grid = (long long)sms * (per > 0 ? per : 1);
+      if (grid > nUnits) grid = nUnits;
+      k_unit_queue<<<(unsigned)grid, kUnitThreads, smemBytes, st>>>(Jc);
+    } else {
+      k_unit_fast<<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(Jc);
+    }
+  }
+  if (u1) record_timing(u1, st);
+  launch_epilogue(Jc, st);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : kLaunchErrorBase + (int)e;
 }
 
 }  // namespace ecpgb

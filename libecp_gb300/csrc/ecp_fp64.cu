@@ -718,11 +718,12 @@ int launch_fp64_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, cud
   if (smemBytes > 200 * 1024) return 3;
   launch_prologue(J, st);
   long long nUnits = (long long)J.nCentres * J.nPairs;
-  if (u0) cudaEventRecord(u0, st);
+  if (u0) record_timing(u0, st);
   if (nUnits > 0) k_unit<<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(J);
-  if (u1) cudaEventRecord(u1, st);
+  if (u1) record_timing(u1, st);
   launch_epilogue(J, st);
-  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : kLaunchErrorBase + (int)e;
 }
 
 // Per-job stages before and after the unit kernel; shared by both paths.

@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -152,6 +153,12 @@ struct DevTables {
 struct Engine {
   std::mutex mu;
   cudaStream_t stream = nullptr;
+  // batched-path launch configuration per (maxLBS, maxLECP), set by the autotuner
+  std::map<std::pair<int, int>, FastConfig> tuned;
+  FastConfig config_for(int LB, int LE) const {
+    auto it = tuned.find({LB, LE});
+    return it == tuned.end() ? FastConfig{} : it->second;
+  }
   std::vector<std::unique_ptr<DevTables>> tables;
   const DevTables *schedOwner = nullptr;
   JobBuffers shared;
@@ -251,9 +258,43 @@ void schedules_overwritten() { engine().schedOwner = nullptr; }
 
 static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// The work queue of the batched path: units by descending estimated cost,
+// primitive pairs x (la + lb + 2) x (L + 2), ties in the reference's order
+// (a stable counting sort).  Empty when the units do not fit 31-bit indices.
+static void unit_order(const Parsed &P, std::vector<int> &order) {
+  order.clear();
+  const long long n = (long long)P.nCentres * P.nPairs;
+  if (n <= 0 || n >= INT_MAX) return;
+  std::vector<int> pk(P.nPairs), ck(P.nCentres);
+  int maxP = 0, maxC = 0;
+  for (int p = 0; p < P.nPairs; p++) {
+    int a = P.pairA[p], b = P.pairB[p];
+    pk[p] = P.shK[a] * P.shK[b] * (P.shL[a] + P.shL[b] + 2);
+    maxP = std::max(maxP, pk[p]);
+  }
+  for (int c = 0; c < P.nCentres; c++) {
+    ck[c] = P.ctrL[c] + 2;
+    maxC = std::max(maxC, ck[c]);
+  }
+  const long long nk = (long long)maxP * maxC + 1;
+  if (nk > (1 << 24)) return;
+  std::vector<int> start(nk + 1, 0);
+  for (int c = 0; c < P.nCentres; c++)
+    for (int p = 0; p < P.nPairs; p++) start[nk - 1 - pk[p] * ck[c]]++;
+  int acc = 0;
+  for (long long k = 0; k <= nk; k++) {
+    int v = start[k];
+    start[k] = acc;
+    acc += v;
+  }
+  order.resize(n);
+  for (int c = 0; c < P.nCentres; c++)
+    for (int p = 0; p < P.nPairs; p++) order[start[nk - 1 - pk[p] * ck[c]]++] = c * P.nPairs + p;
+}
+
 // Packs the inputs into the pinned staging buffer, copies them to the device
 // and fills the DevJob's input and work pointers.
-static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J) {
+static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int mode) {
   const HostTables &h = T->host;
   std::memset(&J, 0, sizeof J);
   J.nAtoms = P.nAtoms; J.nShells = P.nShells; J.nPrims = P.nPrims; J.nCentres = P.nCentres;
@@ -288,6 +329,9 @@ static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers 
          iCT = add(P.ctrT0.data(), 4 * P.ctrT0.size()), iCN = add(P.ctrNT.data(), 4 * P.ctrNT.size()),
          iTL = add(P.termL.data(), 4 * P.termL.size()), iPrA = add(P.pairA.data(), 4 * P.pairA.size()),
          iPrB = add(P.pairB.data(), 4 * P.pairB.size()), iPO = add(P.pairOff.data(), 8 * P.pairOff.size());
+  std::vector<int> order;
+  if (mode == ECPGB_FAST) unit_order(P, order);
+  size_t iOrd = add(order.data(), 4 * order.size());
   if (!B.pinned.ensure(tot) || !B.in.ensure(tot)) {
     set_error("allocation of %zu input bytes failed", tot);
     return -1;
@@ -304,6 +348,7 @@ static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers 
   J.ctrAtom = (const int *)dp(iCA); J.ctrL = (const int *)dp(iCL); J.ctrT0 = (const int *)dp(iCT);
   J.ctrNT = (const int *)dp(iCN); J.termL = (const int *)dp(iTL); J.pairA = (const int *)dp(iPrA);
   J.pairB = (const int *)dp(iPrB); J.pairOff = (const long long *)dp(iPO);
+  J.order = order.empty() ? nullptr : (const int *)dp(iOrd);
   J.centreStride = P.centreStride;
   // --- tables
   J.itemOff = T->itemOff.p; J.itemCnt = T->itemCnt.p; J.items = T->items.p;
@@ -317,35 +362,40 @@ static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers 
             B.cgeo.ensure(nc * na * 4 + 1) && B.usp.ensure(nc * na * J.uspD * J.uspD * J.uspD + 1) &&
             B.ang.ensure(nc * na * (size_t)J.angLam * J.angLM * J.angC + 1) &&
             B.out.ensure(nc * (size_t)P.centreStride + 1) && B.status.ensure(nc * (size_t)P.nPairs + 1) &&
-            B.mat.ensure((size_t)P.dim * P.dim + 1) && B.err.ensure(2);
+            B.mat.ensure((size_t)P.dim * P.dim + 1) && B.err.ensure(2) && B.head.ensure(1);
   if (!ok) {
     set_error("device allocation failed for the job's work arrays");
     return -1;
   }
   J.radius = B.radius.p; J.utab = B.utab.p; J.uL = B.uL.p; J.gridEnd = B.gridEnd.p; J.win = B.win.p;
   J.F = B.F.p; J.cgeo = B.cgeo.p; J.usp = B.usp.p; J.ang = B.ang.p; J.out = B.out.p;
-  J.status = B.status.p; J.mat = B.mat.p; J.errWord = B.err.p;
+  J.status = B.status.p; J.mat = B.mat.p; J.errWord = B.err.p; J.queueHead = B.head.p;
+  J.gcap = FastConfig{}.gcap;
   J.besH = T->besH.p;
   J.besA = T->besA.p;
   J.besHL = h.besselHL;
   J.shNorm = T->shNorm.p;
   UnitSmem L = unit_smem_layout(h.maxLBS, h.maxLECP, h.nF);
   B.smem = sizeof(double) * (size_t)L.total;
-  B.smemFast = fast_smem_bytes(h.maxLBS, h.maxLECP, h.nF);
   return 0;
 }
 
-// Resets the per-run outputs and launches the pipeline of the mode.
+// Resets the per-run outputs and launches the pipeline of the mode (the
+// batched path with launch configuration cfg).
 static int run_pipeline(Engine &E, JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0,
-                        cudaEvent_t u1) {
-  int init[2] = {INT_MAX, 0};
-  std::memcpy(B.pinnedErr, init, sizeof init);
-  CUDA_OK(cudaMemcpyAsync(B.err.p, B.pinnedErr, sizeof init, cudaMemcpyHostToDevice, E.stream));
+                        cudaEvent_t u1, const FastConfig *cfg = nullptr) {
+  launch_reset(J, E.stream);
   CUDA_OK(cudaMemsetAsync(B.mat.p, 0, sizeof(double) * (size_t)J.dim * J.dim, E.stream));
-  int rc = mode == ECPGB_FAST ? launch_fast_pipeline(J, E.stream, B.smemFast, u0, u1)
-                              : launch_fp64_pipeline(J, E.stream, B.smem, u0, u1);
+  int rc;
+  if (mode == ECPGB_FAST) {
+    const FastConfig c = cfg ? *cfg : E.config_for(J.maxLBS, J.maxLECP);
+    rc = launch_fast_pipeline(J, E.stream, fast_smem_bytes(J.maxLBS, J.maxLECP, J.nF, c.gcap), c, u0, u1);
+  } else {
+    rc = launch_fp64_pipeline(J, E.stream, B.smem, u0, u1);
+  }
   if (rc) {
-    set_error("kernel launch failed (%d): %s", rc, cudaGetErrorString(cudaGetLastError()));
+    if (rc >= kLaunchErrorBase) set_error("kernel launch failed: %s", cudaGetErrorString((cudaError_t)(rc - kLaunchErrorBase)));
+    else set_error("kernel launch failed (%d)", rc);
     return -1;
   }
   return 0;
@@ -369,7 +419,7 @@ int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_inf
   if (!T || E.use_schedules(T)) return 1;
   JobBuffers &B = E.shared;
   DevJob J;
-  if (stage_job(E, P, T, B, J)) return 1;
+  if (stage_job(E, P, T, B, J, mode)) return 1;
   cudaEvent_t e0, e1, u0, u1;
   cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
   cudaEventRecord(e0, E.stream);
@@ -421,7 +471,7 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
   if (!T || E.use_schedules(T)) return 1;
   JobBuffers &B = E.shared;
   DevJob J;
-  if (stage_job(E, P, T, B, J)) return 1;
+  if (stage_job(E, P, T, B, J, mode)) return 1;
   const size_t nv = (size_t)P.nCentres * P.centreStride;
   cudaMemsetAsync(B.out.p, 0, sizeof(double) * nv, E.stream);
   cudaEvent_t e0, e1, u0, u1;
@@ -475,9 +525,49 @@ struct ResidentJob {
   const DevTables *T = nullptr;
   JobBuffers B;
   DevJob J;
-  int launches = 6;
+  int launches = 7;  // reset, four per-job stages, the unit kernel, the scatter
   int mode = ECPGB_FP64;
+  FastConfig cfg;
+  bool useGraph = true;
+  // the whole pipeline captured once and replayed per run; gu0/gu1 are
+  // recorded inside it around the unit kernel
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t gu0 = nullptr, gu1 = nullptr;
+  void drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+  }
+  ~ResidentJob() {
+    drop_graph();
+    if (gu0) cudaEventDestroy(gu0);
+    if (gu1) cudaEventDestroy(gu1);
+  }
 };
+
+// Captures the job's pipeline into R->graph (engine lock held).
+static int capture_graph(Engine &E, ResidentJob *R) {
+  if (R->graph) return 0;
+  if (!R->gu0) cudaEventCreate(&R->gu0);
+  if (!R->gu1) cudaEventCreate(&R->gu1);
+  if (R->mode == ECPGB_FAST) fast_prepare();  // function attributes before capture
+  cudaGraph_t g = nullptr;
+  CUDA_OK(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
+  int rc = run_pipeline(E, R->B, R->J, R->mode, R->gu0, R->gu1, &R->cfg);
+  cudaError_t ce = cudaStreamEndCapture(E.stream, &g);
+  if (rc || ce != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    set_error("pipeline capture failed: %s", cudaGetErrorString(ce));
+    return -1;
+  }
+  ce = cudaGraphInstantiate(&R->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) {
+    R->graph = nullptr;
+    set_error("graph instantiation failed: %s", cudaGetErrorString(ce));
+    return -1;
+  }
+  return 0;
+}
 
 void *job_create(const ecpgb_system &s, int mode) {
   Engine &E = engine();
@@ -489,7 +579,10 @@ void *job_create(const ecpgb_system &s, int mode) {
   if (parse_system(s, R->P)) { delete R; return nullptr; }
   if (R->P.nCentres == 0 || R->P.nPairs == 0) { set_error("job has no units"); delete R; return nullptr; }
   R->T = E.get_tables({R->P.maxLECP, R->P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
-  if (!R->T || stage_job(E, R->P, R->T, R->B, R->J)) { delete R; return nullptr; }
+  if (!R->T || stage_job(E, R->P, R->T, R->B, R->J, mode)) { delete R; return nullptr; }
+  R->cfg = E.config_for(R->J.maxLBS, R->J.maxLECP);
+  // skipped units are never written: their values read as zero
+  cudaMemsetAsync(R->B.out.p, 0, sizeof(double) * (size_t)R->P.nCentres * R->P.centreStride, E.stream);
   if (cudaStreamSynchronize(E.stream) != cudaSuccess) { set_error("staging failed"); delete R; return nullptr; }
   return R;
 }
@@ -501,12 +594,41 @@ int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
   if (E.use_schedules(R->T)) return 1;
   const size_t flushBytes = 256u << 20;
   if (flushL2 && !E.flush.ensure(flushBytes)) { set_error("flush buffer allocation failed"); return 1; }
+  if (R->useGraph) {
+    // graph replay: the unit-kernel events live inside the graph, so each
+    // run is read back before the next replay re-records them
+    if (capture_graph(E, R)) return 1;
+    cudaEvent_t a0, a1;
+    cudaEventCreate(&a0);
+    cudaEventCreate(&a1);
+    for (int r = 0; r < nRuns; r++) {
+      if (flushL2) cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
+      cudaEventRecord(a0, E.stream);
+      cudaError_t ce = cudaGraphLaunch(R->graph, E.stream);
+      cudaEventRecord(a1, E.stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(E.stream);
+      if (ce != cudaSuccess) {
+        cudaEventDestroy(a0);
+        cudaEventDestroy(a1);
+        set_error("device error: %s", cudaGetErrorString(ce));
+        return 1;
+      }
+      float a = 0, b = 0;
+      cudaEventElapsedTime(&a, a0, a1);
+      cudaEventElapsedTime(&b, R->gu0, R->gu1);
+      if (msRun) msRun[r] = a;
+      if (msUnit) msUnit[r] = b;
+    }
+    cudaEventDestroy(a0);
+    cudaEventDestroy(a1);
+    return 0;
+  }
   std::vector<cudaEvent_t> ev(4 * nRuns);
   for (auto &e : ev) cudaEventCreate(&e);
   for (int r = 0; r < nRuns; r++) {
     if (flushL2) cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
     cudaEventRecord(ev[4 * r], E.stream);
-    if (run_pipeline(E, R->B, R->J, R->mode, ev[4 * r + 2], ev[4 * r + 3])) return 1;
+    if (run_pipeline(E, R->B, R->J, R->mode, ev[4 * r + 2], ev[4 * r + 3], &R->cfg)) return 1;
     cudaEventRecord(ev[4 * r + 1], E.stream);
   }
   cudaError_t ce = cudaStreamSynchronize(E.stream);
@@ -519,6 +641,101 @@ int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
     if (msUnit) msUnit[r] = b;
   }
   for (auto &e : ev) cudaEventDestroy(e);
+  return 0;
+}
+
+static ecpgb_launch_config to_c(const FastConfig &c, float ms) { return {c.queue, c.sorted, c.gcap, ms}; }
+
+int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials, int *nTrials) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  auto *R = (ResidentJob *)vj;
+  if (nTrials) *nTrials = 0;
+  if (R->mode != ECPGB_FAST) { set_error("the autotuner applies to the batched path only"); return 3; }
+  if (E.use_schedules(R->T)) return 1;
+  // candidates: queue or CTA-per-unit, cost order or the reference's, and
+  // the step-table cap (pairs per warp against CTAs per SM)
+  std::vector<FastConfig> cand;
+  for (int gcap : {45, 64, 33})
+    for (int queue : {1, 0}) cand.push_back(FastConfig{queue, 1, gcap});
+  cand.push_back(FastConfig{0, 0, 45});
+  const size_t flushBytes = 256u << 20;
+  if (!E.flush.ensure(flushBytes)) { set_error("flush buffer allocation failed"); return 1; }
+  cudaEvent_t u0, u1;
+  cudaEventCreate(&u0);
+  cudaEventCreate(&u1);
+  float best = 1e30f;
+  FastConfig bestCfg = R->cfg;
+  int n = 0;
+  for (const FastConfig &c : cand) {
+    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap), c.queue) < 1) continue;
+    float tot = 0;
+    for (int r = 0; r < 3; r++) {
+      cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
+      if (run_pipeline(E, R->B, R->J, R->mode, u0, u1, &c)) { cudaEventDestroy(u0); cudaEventDestroy(u1); return 1; }
+      cudaError_t ce = cudaStreamSynchronize(E.stream);
+      if (ce != cudaSuccess) {
+        cudaEventDestroy(u0);
+        cudaEventDestroy(u1);
+        set_error("device error: %s", cudaGetErrorString(ce));
+        return 1;
+      }
+      float ms = 0;
+      cudaEventElapsedTime(&ms, u0, u1);
+      if (r) tot += ms;
+    }
+    float ms = tot / 2;
+    if (trials && n < maxTrials) trials[n] = to_c(c, ms);
+    n++;
+    if (ms < best) { best = ms; bestCfg = c; }
+  }
+  cudaEventDestroy(u0);
+  cudaEventDestroy(u1);
+  if (nTrials) *nTrials = n < maxTrials ? n : maxTrials;
+  R->cfg = bestCfg;
+  R->drop_graph();
+  E.tuned[{R->J.maxLBS, R->J.maxLECP}] = bestCfg;
+  if (chosen) *chosen = to_c(bestCfg, best);
+  return 0;
+}
+
+int job_config(void *vj, const ecpgb_launch_config *cfg, ecpgb_launch_config *out) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  auto *R = (ResidentJob *)vj;
+  if (cfg) {
+    if (R->mode != ECPGB_FAST) { set_error("launch configurations apply to the batched path only"); return 3; }
+    if (cfg->gcap < 1 || cfg->gcap > 4096) { set_error("gcap %d out of range", cfg->gcap); return 1; }
+    FastConfig c{cfg->queue ? 1 : 0, cfg->sorted ? 1 : 0, cfg->gcap};
+    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap), c.queue) < 1) {
+      set_error("configuration does not fit on an SM");
+      return 1;
+    }
+    R->cfg = c;
+    R->drop_graph();
+  }
+  if (out) *out = to_c(R->cfg, 0.0f);
+  return 0;
+}
+
+int job_blocks(void *vj, double *values, int *status) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  auto *R = (ResidentJob *)vj;
+  const size_t nv = (size_t)R->P.nCentres * R->P.centreStride, nu = (size_t)R->P.nCentres * R->P.nPairs;
+  if (values) cudaMemcpyAsync(values, R->B.out.p, sizeof(double) * nv, cudaMemcpyDeviceToHost, E.stream);
+  if (status) cudaMemcpyAsync(status, R->B.status.p, sizeof(int) * nu, cudaMemcpyDeviceToHost, E.stream);
+  cudaError_t ce = cudaStreamSynchronize(E.stream);
+  if (ce != cudaSuccess) { set_error("copy failed: %s", cudaGetErrorString(ce)); return 1; }
+  return 0;
+}
+
+int job_use_graph(void *vj, int on) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  auto *R = (ResidentJob *)vj;
+  R->useGraph = on != 0;
+  if (!R->useGraph) R->drop_graph();
   return 0;
 }
 

@@ -81,6 +81,7 @@ struct JobBuffers {
   DBuf<char> in;
   DBuf<double> radius, utab, uL, F, cgeo, usp, ang, out, mat;
   DBuf<int> gridEnd, win, status, err;
+  DBuf<unsigned long long> head;
   PinnedBuf pinned, pinnedOut;
   int *pinnedErr = nullptr;
   size_t smem = 0, smemFast = 0;
@@ -101,6 +102,10 @@ int job_matrix(void *j, int rowdim, double *I);
 long long job_units(const void *j, long long *emitted);
 int job_launches(const void *j);
 void job_free(void *j);
+int job_tune(void *j, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials, int *nTrials);
+int job_config(void *j, const ecpgb_launch_config *cfg, ecpgb_launch_config *out);
+int job_use_graph(void *j, int on);
+int job_blocks(void *j, double *values, int *status);
 int measure_peaks(double *out);
 
 // The engine's lock (serialises every use of the shared __constant__ level

@@ -1,0 +1,93 @@
+"""The batched engine's launch machinery: the persistent work-queue launch,
+the cost-ordered queue, the captured CUDA graph and the autotuner.
+
+queue / sorted / graph change only where and when units run, so the values
+must agree bit for bit; gcap regroups the type-1 sums over warps (rounding
+level), and every configuration stays within the parity bar of the FP64 path."""
+import numpy as np
+import pytest
+
+from libecp_gb300 import workloads as W
+from tests.helpers import TOL_ABS
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eg():
+    import libecp_gb300
+    libecp_gb300.lib()
+    return libecp_gb300
+
+
+@pytest.fixture(scope="module")
+def system():
+    return W.batched_cluster(0).subset(centres=list(range(6)))
+
+
+def _run(eg, job, **cfg):
+    if cfg:
+        job.config(**cfg)
+    job.run(1, flush_l2=False)
+    return job.blocks()
+
+
+def test_queue_order_and_graph_are_bitwise_neutral(eg, system):
+    j = eg.Job(system, mode=eg.ECPGB_FAST)
+    base_v, base_s = _run(eg, j, queue=1, sorted=1, gcap=45)
+    for cfg in ({"queue": 0, "sorted": 1}, {"queue": 0, "sorted": 0}, {"queue": 1, "sorted": 0}):
+        v, s = _run(eg, j, gcap=45, **cfg)
+        assert np.array_equal(s, base_s), cfg
+        assert np.array_equal(v, base_v), cfg
+    j.config(queue=1, sorted=1, gcap=45)
+    j.use_graph(False)
+    v, s = _run(eg, j)
+    assert np.array_equal(v, base_v) and np.array_equal(s, base_s)
+    j.use_graph(True)
+    for _ in range(2):  # replays of one captured graph
+        v, s = _run(eg, j)
+        assert np.array_equal(v, base_v) and np.array_equal(s, base_s)
+    j.close()
+
+
+def test_every_config_within_parity_of_fp64(eg, system):
+    jp = eg.Job(system, mode=eg.ECPGB_FP64)
+    ref_v, ref_s = _run(eg, jp)
+    jp.close()
+    j = eg.Job(system, mode=eg.ECPGB_FAST)
+    for gcap in (33, 45, 64):
+        v, s = _run(eg, j, queue=1, sorted=1, gcap=gcap)
+        assert np.array_equal(s, ref_s), gcap
+        err = np.abs(v - ref_v).max()  # skipped units read zero in both
+        assert err <= TOL_ABS, (gcap, err)
+    j.close()
+
+
+def test_autotuner_picks_a_measured_candidate(eg, system):
+    j = eg.Job(system, mode=eg.ECPGB_FAST)
+    chosen, trials = j.tune()
+    assert len(trials) >= 4
+    assert all(t["msUnit"] > 0 for t in trials)
+    best = min(trials, key=lambda t: t["msUnit"])
+    assert (chosen["queue"], chosen["sorted"], chosen["gcap"]) == (best["queue"], best["sorted"], best["gcap"])
+    cur = j.config()
+    assert (cur["queue"], cur["sorted"], cur["gcap"]) == (chosen["queue"], chosen["sorted"], chosen["gcap"])
+    # the tuned job still matches the drop-in matrix path
+    ms, _ = j.run(1)
+    I1 = j.matrix()
+    rc, I2, _ = eg.get_integrals_info(system, mode=eg.ECPGB_FP64)
+    assert np.abs(I1 - np.triu(I2)).max() <= TOL_ABS
+    j.close()
+
+
+def test_tuner_rejects_the_plain_path(eg, system):
+    j = eg.Job(system, mode=eg.ECPGB_FP64)
+    with pytest.raises(RuntimeError):
+        j.tune()
+    j.close()
+
+
+def test_launches_per_run(eg, system):
+    j = eg.Job(system, mode=eg.ECPGB_FAST)
+    assert j.launches_per_run() == 7
+    j.close()
