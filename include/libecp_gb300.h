@@ -123,6 +123,41 @@ int ecpgb_job_use_graph(ecpgb_job *j, int on);
  * either pointer may be NULL. */
 int ecpgb_job_blocks(ecpgb_job *j, double *values, int *status);
 
+/* Request server (continuous batching).  A worker thread admits submitted
+ * jobs in arrival order as slots and device memory free up: each admitted
+ * job is staged and run on its own CUDA stream while earlier ones are still
+ * on the GPU, so their kernels overlap; the device-resident tables are shared
+ * by all of them.  hbmBudgetBytes caps the device bytes the slots hold (a job
+ * larger than the budget fails); slots caps the jobs in flight (1..64).  mode
+ * is ECPGB_FP64 or ECPGB_FAST for every job of the server.  Results are those
+ * of ecpgb_getIntegrals for the same system, mode and launch configuration,
+ * bit for bit: a job runs the same kernels in the mix as alone. */
+typedef struct ecpgb_server ecpgb_server;
+typedef struct {
+  long long units, values;  /* (pair, centre) units and block values of the job */
+  double msQueued;          /* submit -> admitted (host clock) */
+  double msLatency;         /* submit -> result ready (host clock) */
+  double msGpu;             /* CUDA events around the job's stream work */
+  long long deviceBytes;    /* device bytes of the job's slot while it ran */
+  int slot, firstFailed;    /* firstFailed: first unit with a warning, -1 none */
+} ecpgb_request_info;
+typedef struct {
+  long long submitted, completed, failed, queued, inflight;
+  long long deviceBytesHeld, budget;
+  int slots, maxInflight; /* maxInflight: most jobs seen on the GPU at once */
+} ecpgb_server_stats;
+ecpgb_server *ecpgb_server_create(int mode, long long hbmBudgetBytes, int slots);
+/* Copies the system; returns the request id (>= 0) or -1 (see ecpgb_last_error). */
+long long ecpgb_server_submit(ecpgb_server *sv, const ecpgb_system *s);
+/* 0 queued or running, 1 done, -1 unknown id or failed. */
+int ecpgb_server_poll(ecpgb_server *sv, long long id);
+/* Blocks until the request is done, then I += its upper triangle (row stride
+ * rowdim) and the request is released.  Returns like ecpgb_getIntegrals. */
+int ecpgb_server_wait(ecpgb_server *sv, long long id, int rowdim, double *I, ecpgb_request_info *info);
+int ecpgb_server_get_stats(ecpgb_server *sv, ecpgb_server_stats *st);
+/* Finishes the jobs in flight and queued, then frees the server. */
+void ecpgb_server_free(ecpgb_server *sv);
+
 /* Pipe-throughput probe on the current device: out[0] FP64 FMA TFLOP/s,
  * out[1] FP32 FMA TFLOP/s, out[2] MUFU ex2 Gop/s, out[3] FP64 exp() Gop/s.
  * Takes about 0.5 s.  0 ok. */

@@ -53,6 +53,26 @@ class LaunchConfig(ct.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class RequestInfo(ct.Structure):
+    """ecpgb_request_info: one served request."""
+    _fields_ = [("units", ct.c_longlong), ("values", ct.c_longlong), ("msQueued", ct.c_double),
+                ("msLatency", ct.c_double), ("msGpu", ct.c_double), ("deviceBytes", ct.c_longlong),
+                ("slot", ct.c_int), ("firstFailed", ct.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class ServerStats(ct.Structure):
+    """ecpgb_server_stats."""
+    _fields_ = [("submitted", ct.c_longlong), ("completed", ct.c_longlong), ("failed", ct.c_longlong),
+                ("queued", ct.c_longlong), ("inflight", ct.c_longlong), ("deviceBytesHeld", ct.c_longlong),
+                ("budget", ct.c_longlong), ("slots", ct.c_int), ("maxInflight", ct.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 ECP_CALLBACK = ct.CFUNCTYPE(None, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
                             ct.c_int, ct.c_int, ct.c_int, _D, ct.c_void_p)
 
@@ -101,6 +121,18 @@ def lib() -> ct.CDLL:
     L.ecpgb_job_use_graph.restype = ct.c_int
     L.ecpgb_job_blocks.argtypes = [ct.c_void_p, _D, _I]
     L.ecpgb_job_blocks.restype = ct.c_int
+    L.ecpgb_server_create.argtypes = [ct.c_int, ct.c_longlong, ct.c_int]
+    L.ecpgb_server_create.restype = ct.c_void_p
+    L.ecpgb_server_submit.argtypes = [ct.c_void_p, P]
+    L.ecpgb_server_submit.restype = ct.c_longlong
+    L.ecpgb_server_poll.argtypes = [ct.c_void_p, ct.c_longlong]
+    L.ecpgb_server_poll.restype = ct.c_int
+    L.ecpgb_server_wait.argtypes = [ct.c_void_p, ct.c_longlong, ct.c_int, _D, ct.POINTER(RequestInfo)]
+    L.ecpgb_server_wait.restype = ct.c_int
+    L.ecpgb_server_get_stats.argtypes = [ct.c_void_p, ct.POINTER(ServerStats)]
+    L.ecpgb_server_get_stats.restype = ct.c_int
+    L.ecpgb_server_free.argtypes = [ct.c_void_p]
+    L.ecpgb_server_free.restype = None
     L.ecpgb_job_free.restype = None
     L.ecpgb_measure_peaks.argtypes = [_D]
     L.ecpgb_last_error.restype = ct.c_char_p
@@ -332,3 +364,58 @@ def measure_peaks() -> dict:
         raise RuntimeError(last_error())
     return {"fp64_fma_tflops": out[0], "fp32_fma_tflops": out[1], "mufu_ex2_gops": out[2],
             "fp64_exp_gops": out[3]}
+
+
+class Server:
+    """Request server with continuous batching (ecpgb_server_*): jobs are
+    admitted in arrival order as slots and device memory free up, and run on
+    their own streams while earlier jobs are still on the GPU."""
+
+    def __init__(self, mode: int = ECPGB_FAST, budget_bytes: int = 8 << 30, slots: int = 8):
+        self._h = lib().ecpgb_server_create(mode, int(budget_bytes), int(slots))
+        if not self._h:
+            raise RuntimeError(f"ecpgb_server_create failed: {last_error()}")
+        self._dims = {}
+
+    def submit(self, s: EcpSystem) -> int:
+        cs = c_system(s)
+        rid = lib().ecpgb_server_submit(self._h, ct.byref(cs))
+        if rid < 0:
+            raise RuntimeError(f"ecpgb_server_submit failed: {last_error()}")
+        self._dims[rid] = s.dim
+        return rid
+
+    def poll(self, rid: int) -> int:
+        return lib().ecpgb_server_poll(self._h, rid)
+
+    def wait(self, rid: int):
+        """(rc, upper-triangle matrix, info dict); raises on failure."""
+        dim = self._dims.pop(rid)
+        I = np.zeros((dim, dim))
+        info = RequestInfo()
+        rc = lib().ecpgb_server_wait(self._h, rid, dim, I.ctypes.data_as(_D), ct.byref(info))
+        if rc == 1:
+            raise RuntimeError(f"request {rid} failed: {last_error()}")
+        return rc, I, info.as_dict()
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        lib().ecpgb_server_get_stats(self._h, ct.byref(st))
+        return st.as_dict()
+
+    def close(self):
+        if self._h:
+            lib().ecpgb_server_free(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -28,6 +28,7 @@ UNITS = [
     ("ecp_capi.cpp", []),
     ("ecp_noalloc.cu", []),
     ("ecp_fast.cu", []),
+    ("ecp_serve.cpp", []),
 ]
 
 

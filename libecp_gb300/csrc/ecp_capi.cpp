@@ -225,6 +225,36 @@ int ecpgb_job_blocks(ecpgb_job *j, double *values, int *status) {
   return j ? ecpgb::job_blocks(j->impl, values, status) : 1;
 }
 
+struct ecpgb_server {
+  void *impl;
+};
+
+ecpgb_server *ecpgb_server_create(int mode, long long hbmBudgetBytes, int slots) {
+  void *impl = ecpgb::server_create(mode, hbmBudgetBytes, slots);
+  return impl ? new ecpgb_server{impl} : nullptr;
+}
+
+long long ecpgb_server_submit(ecpgb_server *sv, const ecpgb_system *s) {
+  if (!sv || !s) { ecpgb::set_error("null server or system"); return -1; }
+  return ecpgb::server_submit(sv->impl, *s);
+}
+
+int ecpgb_server_poll(ecpgb_server *sv, long long id) { return sv ? ecpgb::server_poll(sv->impl, id) : -1; }
+
+int ecpgb_server_wait(ecpgb_server *sv, long long id, int rowdim, double *I, ecpgb_request_info *info) {
+  return sv ? ecpgb::server_wait(sv->impl, id, rowdim, I, info) : 1;
+}
+
+int ecpgb_server_get_stats(ecpgb_server *sv, ecpgb_server_stats *st) {
+  return sv && st ? ecpgb::server_stats(sv->impl, st) : 1;
+}
+
+void ecpgb_server_free(ecpgb_server *sv) {
+  if (!sv) return;
+  ecpgb::server_free(sv->impl);
+  delete sv;
+}
+
 void ecpgb_job_free(ecpgb_job *j) {
   if (!j) return;
   ecpgb::job_free(j->impl);

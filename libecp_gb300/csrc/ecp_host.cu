@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <condition_variable>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -150,6 +151,12 @@ struct DevTables {
   int nItemsMax = 0;
 };
 
+// Two table sets share level schedules when their grids are the same.
+static bool same_schedules(const DevTables *a, const DevTables *b) {
+  return a->host.s93.slot == b->host.s93.slot && a->host.s92.slot == b->host.s92.slot &&
+         a->host.s93.lvEnd == b->host.s93.lvEnd && a->host.s92.lvEnd == b->host.s92.lvEnd;
+}
+
 struct Engine {
   std::mutex mu;
   cudaStream_t stream = nullptr;
@@ -180,6 +187,10 @@ struct Engine {
   const DevTables *get_tables(const TableKey &key) {
     for (auto &t : tables)
       if (t->key == key) return t.get();
+    if (tables.size() >= 256) {
+      set_error("more than 256 distinct table keys (ECP L, basis l, grid order, accuracy)");
+      return nullptr;
+    }
     auto t = std::make_unique<DevTables>();
     t->key = key;
     build_tables(key, t->host);
@@ -220,13 +231,32 @@ struct Engine {
       set_error("angular momenta too high for the FP64 kernel (%d radial items)", t->nItemsMax);
       return nullptr;
     }
-    if (tables.size() >= 8) tables.erase(tables.begin());
+    // tables live as long as the process: resident jobs and requests in
+    // flight hold pointers to them
     tables.push_back(std::move(t));
     return tables.back().get();
   }
 
-  int use_schedules(const DevTables *t) {
+  // Requests in flight on the server's streams pin the current schedules;
+  // a caller that needs other schedules waits (lock held by the caller,
+  // passed in so the wait can release it) until no pin is left.
+  int schedPins = 0;
+  std::condition_variable cv;
+
+  int use_schedules(const DevTables *t, std::unique_lock<std::mutex> *lk = nullptr) {
     if (schedOwner == t) return 0;
+    if (schedOwner && same_schedules(schedOwner, t)) {
+      schedOwner = t;
+      return 0;
+    }
+    if (schedPins > 0) {
+      if (!lk) {
+        set_error("level schedules are pinned by requests in flight");
+        return -1;
+      }
+      cv.wait(*lk, [&] { return schedPins == 0; });
+      if (schedOwner == t) return 0;
+    }
     const HostTables &h = t->host;
     int rc = upload_schedules(h.s93.slot.data(), (int)h.s93.slot.size(), h.s93.lvEnd.data(),
                               h.s93.lvJ.data(), h.s93.lvN.data(), h.s93.nLevels, h.s92.slot.data(),
@@ -253,6 +283,27 @@ static Engine &engine() {
 
 std::mutex &engine_mutex() { return engine().mu; }
 void schedules_overwritten() { engine().schedOwner = nullptr; }
+int engine_pin_request(const Parsed &P, const DevTables **T) {
+  Engine &E = engine();
+  if (E.ensure_init()) return 1;
+  const DevTables *t = E.get_tables({P.maxLECP, P.maxLBS, P.largeGridOrder, P.tol, P.acc});
+  if (!t) return 1;
+  if (E.schedPins > 0 && E.schedOwner != t && !(E.schedOwner && same_schedules(E.schedOwner, t))) return 4;
+  if (E.use_schedules(t)) return 1;
+  E.schedPins++;
+  *T = t;
+  return 0;
+}
+
+void engine_unpin_request() {
+  Engine &E = engine();
+  if (E.schedPins > 0 && --E.schedPins == 0) E.cv.notify_all();
+}
+
+void wait_schedules_unpinned(std::unique_lock<std::mutex> &lk) {
+  Engine &E = engine();
+  E.cv.wait(lk, [&] { return E.schedPins == 0; });
+}
 
 // ------------------------------------------------------------ job set-up
 
@@ -294,7 +345,21 @@ static void unit_order(const Parsed &P, std::vector<int> &order) {
 
 // Packs the inputs into the pinned staging buffer, copies them to the device
 // and fills the DevJob's input and work pointers.
-static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int mode) {
+size_t job_device_bytes(const Parsed &P, int mode) {
+  const size_t nc = P.nCentres, ns = P.nShells, na = P.nAtoms, O = kSmallOrder;
+  const size_t LE = P.maxLECP > 0 ? P.maxLECP : 1, LB = P.maxLBS;
+  const size_t nk = std::max(LB + LE, 2 * LB) + 1, nF = LB + LE + 1, D = LB + 1;  // table ranks (upper bounds)
+  const size_t angLam = P.maxLECP + LB + 1, angC = (LB + 1) * (LB + 2) * (LB + 3) / 6;
+  size_t in = 8 * (P.geom.size() + P.primA.size() + P.primD.size() + 3 * P.termL.size() + P.pairOff.size()) +
+              4 * (5 * P.shL.size() + P.atomMaxL.size() + 4 * P.ctrAtom.size() + P.termL.size() + 2 * P.pairA.size()) +
+              (mode == ECPGB_FAST ? 4 * nc * P.nPairs : 0) + 21 * 256;
+  size_t work = 8 * (ns + nc * O * LE * nk + nc * O + nc * ns * O * nF + nc * na * 4 + nc * na * D * D * D +
+                     nc * na * angLam * LE * LE * angC + nc * (size_t)P.centreStride + (size_t)P.dim * P.dim) +
+                4 * (nc + nc * ns * 3 + nc * (size_t)P.nPairs + 2) + 8;
+  return in + work;
+}
+
+int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int mode, cudaStream_t stream) {
   const HostTables &h = T->host;
   std::memset(&J, 0, sizeof J);
   J.nAtoms = P.nAtoms; J.nShells = P.nShells; J.nPrims = P.nPrims; J.nCentres = P.nCentres;
@@ -338,7 +403,7 @@ static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers 
   }
   for (auto &p : pcs)
     if (p.bytes) std::memcpy(B.pinned.p + p.off, p.src, p.bytes);
-  CUDA_OK(cudaMemcpyAsync(B.in.p, B.pinned.p, tot, cudaMemcpyHostToDevice, E.stream));
+  CUDA_OK(cudaMemcpyAsync(B.in.p, B.pinned.p, tot, cudaMemcpyHostToDevice, stream));
   B.h2dBytes = (long long)tot;
   auto dp = [&](size_t i) { return (void *)(B.in.p + pcs[i].off); };
   J.geom = (const double *)dp(iGeom); J.primA = (const double *)dp(iPA); J.primD = (const double *)dp(iPD);
@@ -382,16 +447,16 @@ static int stage_job(Engine &E, const Parsed &P, const DevTables *T, JobBuffers 
 
 // Resets the per-run outputs and launches the pipeline of the mode (the
 // batched path with launch configuration cfg).
-static int run_pipeline(Engine &E, JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0,
-                        cudaEvent_t u1, const FastConfig *cfg = nullptr) {
-  launch_reset(J, E.stream);
-  CUDA_OK(cudaMemsetAsync(B.mat.p, 0, sizeof(double) * (size_t)J.dim * J.dim, E.stream));
+int run_pipeline(JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0, cudaEvent_t u1,
+                 const FastConfig *cfg, cudaStream_t stream) {
+  launch_reset(J, stream);
+  CUDA_OK(cudaMemsetAsync(B.mat.p, 0, sizeof(double) * (size_t)J.dim * J.dim, stream));
   int rc;
   if (mode == ECPGB_FAST) {
-    const FastConfig c = cfg ? *cfg : E.config_for(J.maxLBS, J.maxLECP);
-    rc = launch_fast_pipeline(J, E.stream, fast_smem_bytes(J.maxLBS, J.maxLECP, J.nF, c.gcap), c, u0, u1);
+    const FastConfig c = cfg ? *cfg : engine().config_for(J.maxLBS, J.maxLECP);
+    rc = launch_fast_pipeline(J, stream, fast_smem_bytes(J.maxLBS, J.maxLECP, J.nF, c.gcap), c, u0, u1);
   } else {
-    rc = launch_fp64_pipeline(J, E.stream, B.smem, u0, u1);
+    rc = launch_fp64_pipeline(J, stream, B.smem, u0, u1);
   }
   if (rc) {
     if (rc >= kLaunchErrorBase) set_error("kernel launch failed: %s", cudaGetErrorString((cudaError_t)(rc - kLaunchErrorBase)));
@@ -405,7 +470,7 @@ static int run_pipeline(Engine &E, JobBuffers &B, const DevJob &J, int mode, cud
 
 int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_info *info) {
   Engine &E = engine();
-  std::lock_guard<std::mutex> lk(E.mu);
+  std::unique_lock<std::mutex> lk(E.mu);
   if (mode != ECPGB_FP64 && mode != ECPGB_FAST) { set_error("unknown mode %d", mode); return 1; }
   if (E.ensure_init()) return 1;
   Parsed P;
@@ -416,14 +481,14 @@ int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_inf
     return 0;
   }
   const DevTables *T = E.get_tables({P.maxLECP, P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
-  if (!T || E.use_schedules(T)) return 1;
+  if (!T || E.use_schedules(T, &lk)) return 1;
   JobBuffers &B = E.shared;
   DevJob J;
-  if (stage_job(E, P, T, B, J, mode)) return 1;
+  if (stage_job(P, T, B, J, mode, E.stream)) return 1;
   cudaEvent_t e0, e1, u0, u1;
   cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
   cudaEventRecord(e0, E.stream);
-  if (run_pipeline(E, B, J, mode, u0, u1)) return 1;
+  if (run_pipeline(B, J, mode, u0, u1, nullptr, E.stream)) return 1;
   cudaEventRecord(e1, E.stream);
   size_t mb = sizeof(double) * (size_t)P.dim * P.dim;
   if (!B.pinnedOut.ensure(mb)) { set_error("pinned allocation failed"); return 1; }
@@ -456,7 +521,7 @@ int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_inf
 int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offsets, int *status,
                ecpgb_info *info, Parsed *parsedOut) {
   Engine &E = engine();
-  std::lock_guard<std::mutex> lk(E.mu);
+  std::unique_lock<std::mutex> lk(E.mu);
   if (mode != ECPGB_FP64 && mode != ECPGB_FAST) { set_error("unknown mode %d", mode); return 1; }
   if (E.ensure_init()) return 1;
   Parsed P;
@@ -468,16 +533,16 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
     return 0;
   }
   const DevTables *T = E.get_tables({P.maxLECP, P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
-  if (!T || E.use_schedules(T)) return 1;
+  if (!T || E.use_schedules(T, &lk)) return 1;
   JobBuffers &B = E.shared;
   DevJob J;
-  if (stage_job(E, P, T, B, J, mode)) return 1;
+  if (stage_job(P, T, B, J, mode, E.stream)) return 1;
   const size_t nv = (size_t)P.nCentres * P.centreStride;
   cudaMemsetAsync(B.out.p, 0, sizeof(double) * nv, E.stream);
   cudaEvent_t e0, e1, u0, u1;
   cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
   cudaEventRecord(e0, E.stream);
-  if (run_pipeline(E, B, J, mode, u0, u1)) return 1;
+  if (run_pipeline(B, J, mode, u0, u1, nullptr, E.stream)) return 1;
   cudaEventRecord(e1, E.stream);
   if (values) cudaMemcpyAsync(values, B.out.p, sizeof(double) * nv, cudaMemcpyDeviceToHost, E.stream);
   std::vector<int> st(nUnits);
@@ -552,7 +617,7 @@ static int capture_graph(Engine &E, ResidentJob *R) {
   if (R->mode == ECPGB_FAST) fast_prepare();  // function attributes before capture
   cudaGraph_t g = nullptr;
   CUDA_OK(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
-  int rc = run_pipeline(E, R->B, R->J, R->mode, R->gu0, R->gu1, &R->cfg);
+  int rc = run_pipeline(R->B, R->J, R->mode, R->gu0, R->gu1, &R->cfg, E.stream);
   cudaError_t ce = cudaStreamEndCapture(E.stream, &g);
   if (rc || ce != cudaSuccess || !g) {
     if (g) cudaGraphDestroy(g);
@@ -579,7 +644,7 @@ void *job_create(const ecpgb_system &s, int mode) {
   if (parse_system(s, R->P)) { delete R; return nullptr; }
   if (R->P.nCentres == 0 || R->P.nPairs == 0) { set_error("job has no units"); delete R; return nullptr; }
   R->T = E.get_tables({R->P.maxLECP, R->P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
-  if (!R->T || stage_job(E, R->P, R->T, R->B, R->J, mode)) { delete R; return nullptr; }
+  if (!R->T || stage_job(R->P, R->T, R->B, R->J, mode, E.stream)) { delete R; return nullptr; }
   R->cfg = E.config_for(R->J.maxLBS, R->J.maxLECP);
   // skipped units are never written: their values read as zero
   cudaMemsetAsync(R->B.out.p, 0, sizeof(double) * (size_t)R->P.nCentres * R->P.centreStride, E.stream);
@@ -589,9 +654,9 @@ void *job_create(const ecpgb_system &s, int mode) {
 
 int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
   Engine &E = engine();
-  std::lock_guard<std::mutex> lk(E.mu);
+  std::unique_lock<std::mutex> lk(E.mu);
   auto *R = (ResidentJob *)vj;
-  if (E.use_schedules(R->T)) return 1;
+  if (E.use_schedules(R->T, &lk)) return 1;
   const size_t flushBytes = 256u << 20;
   if (flushL2 && !E.flush.ensure(flushBytes)) { set_error("flush buffer allocation failed"); return 1; }
   if (R->useGraph) {
@@ -628,7 +693,7 @@ int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
   for (int r = 0; r < nRuns; r++) {
     if (flushL2) cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
     cudaEventRecord(ev[4 * r], E.stream);
-    if (run_pipeline(E, R->B, R->J, R->mode, ev[4 * r + 2], ev[4 * r + 3], &R->cfg)) return 1;
+    if (run_pipeline(R->B, R->J, R->mode, ev[4 * r + 2], ev[4 * r + 3], &R->cfg, E.stream)) return 1;
     cudaEventRecord(ev[4 * r + 1], E.stream);
   }
   cudaError_t ce = cudaStreamSynchronize(E.stream);
@@ -648,11 +713,11 @@ static ecpgb_launch_config to_c(const FastConfig &c, float ms) { return {c.queue
 
 int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials, int *nTrials) {
   Engine &E = engine();
-  std::lock_guard<std::mutex> lk(E.mu);
+  std::unique_lock<std::mutex> lk(E.mu);
   auto *R = (ResidentJob *)vj;
   if (nTrials) *nTrials = 0;
   if (R->mode != ECPGB_FAST) { set_error("the autotuner applies to the batched path only"); return 3; }
-  if (E.use_schedules(R->T)) return 1;
+  if (E.use_schedules(R->T, &lk)) return 1;
   // candidates: queue or CTA-per-unit, cost order or the reference's, and
   // the step-table cap (pairs per warp against CTAs per SM)
   std::vector<FastConfig> cand;
@@ -672,7 +737,7 @@ int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials,
     float tot = 0;
     for (int r = 0; r < 3; r++) {
       cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
-      if (run_pipeline(E, R->B, R->J, R->mode, u0, u1, &c)) { cudaEventDestroy(u0); cudaEventDestroy(u1); return 1; }
+      if (run_pipeline(R->B, R->J, R->mode, u0, u1, &c, E.stream)) { cudaEventDestroy(u0); cudaEventDestroy(u1); return 1; }
       cudaError_t ce = cudaStreamSynchronize(E.stream);
       if (ce != cudaSuccess) {
         cudaEventDestroy(u0);

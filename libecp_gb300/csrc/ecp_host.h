@@ -4,8 +4,10 @@
 
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
+#include "ecp_engine.h"
 #include "libecp_gb300.h"
 
 namespace ecpgb {
@@ -87,6 +89,11 @@ struct JobBuffers {
   size_t smem = 0, smemFast = 0;
   long long h2dBytes = 0;
   JobBuffers() { cudaMallocHost((void **)&pinnedErr, 4 * sizeof(int)); }
+  // device bytes held by the buffers
+  size_t device_bytes() const {
+    return in.cap + 8 * (radius.cap + utab.cap + uL.cap + F.cap + cgeo.cap + usp.cap + ang.cap + out.cap + mat.cap) +
+           4 * (gridEnd.cap + win.cap + status.cap + err.cap) + 8 * head.cap;
+  }
   ~JobBuffers() {
     if (pinnedErr) cudaFreeHost(pinnedErr);
   }
@@ -113,6 +120,34 @@ int measure_peaks(double *out);
 // schedules itself, so the engine re-uploads its own before its next run.
 std::mutex &engine_mutex();
 void schedules_overwritten();
+// Waits (releasing lk, which holds the engine lock) until no request in
+// flight pins the level schedules.
+void wait_schedules_unpinned(std::unique_lock<std::mutex> &lk);
 int run_matrix_noalloc(const ecpgb_system &s, int rowdim, double *I);
+
+// ---- internals shared with the request server (ecp_serve.cpp)
+struct DevTables;
+// Packs P's inputs into B's pinned buffer, copies them to the device on
+// `stream` and fills J (B's buffers grow as needed).
+int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int mode, cudaStream_t stream);
+// Resets the run's words and launches the pipeline of the mode on `stream`;
+// cfg null = the tuned configuration for the job's (l, L).
+int run_pipeline(JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0, cudaEvent_t u1,
+                 const FastConfig *cfg, cudaStream_t stream);
+// Device bytes a job of P will hold (inputs and work arrays).
+size_t job_device_bytes(const Parsed &P, int mode);
+// With the engine lock held: the tables of the request and, unless requests
+// in flight pin other level schedules (returns 4: retry after they finish),
+// its schedules made current and pinned.  0 ok, 1 error.
+int engine_pin_request(const Parsed &P, const DevTables **T);
+// With the engine lock held: releases one pin.
+void engine_unpin_request();
+// Server objects (ecp_serve.cpp).
+void *server_create(int mode, long long budget, int slots);
+long long server_submit(void *sv, const ecpgb_system &s);
+int server_poll(void *sv, long long id);
+int server_wait(void *sv, long long id, int rowdim, double *I, ecpgb_request_info *info);
+int server_stats(void *sv, ecpgb_server_stats *st);
+void server_free(void *sv);
 
 }  // namespace ecpgb

@@ -82,7 +82,7 @@ static bool put(T *dst, const std::vector<T> &v) {
 }
 
 int run_matrix_noalloc(const ecpgb_system &s, int rowdim, double *I) {
-  std::lock_guard<std::mutex> lk(engine_mutex());
+  std::unique_lock<std::mutex> lk(engine_mutex());
   Parsed P;
   if (parse_system(s, P)) return 1;
   if (rowdim < P.dim) { set_error("rowdim %d < basis dimension %d", rowdim, P.dim); return 1; }
@@ -193,6 +193,8 @@ int run_matrix_noalloc(const ecpgb_system &s, int rowdim, double *I) {
   J.itemOff = iO; J.itemCnt = iC; J.items = iI;
 
   // the level schedules live in __constant__ memory shared with the engine
+  // (and with requests in flight on the server's streams: wait for those)
+  wait_schedules_unpinned(lk);
   if (upload_schedules(h.s93.slot.data(), (int)h.s93.slot.size(), h.s93.lvEnd.data(), h.s93.lvJ.data(),
                        h.s93.lvN.data(), h.s93.nLevels, h.s92.slot.data(), (int)h.s92.slot.size(),
                        h.s92.lvEnd.data(), h.s92.lvN.data(), h.s92.nLevels, nullptr)) {

@@ -41,9 +41,10 @@ struct Schedule {
 struct TableKey {
   int maxLECP, maxLBS, largeGridOrder;
   double tolerance, accuracy;
+  // the tables do not depend on the quadrature tolerance
   bool operator==(const TableKey &o) const {
     return maxLECP == o.maxLECP && maxLBS == o.maxLBS && largeGridOrder == o.largeGridOrder &&
-           tolerance == o.tolerance && accuracy == o.accuracy;
+           accuracy == o.accuracy;
   }
 };
 
