@@ -37,6 +37,15 @@ enum {
                        points tabulated level by level until convergence,
                        Horner-form Bessel rows, table-driven exp; same
                        schedules and decisions, rounding-level differences */
+  ECPGB_MIXED = 2,  /* the batched path with the bulk radial arithmetic in
+                       FP32: Bessel rows below the large-argument branch
+                       (Horner in FP32 over FP32 Taylor coefficients) and the
+                       ECP channel terms d r^n exp(-a r^2) (FP32 exp).  FP64
+                       stays for the large-argument Bessel rows, the Gaussian
+                       product exp prefactors, the quadrature sums and their
+                       convergence tests, and every accumulation.  Errors are
+                       those of FP32 (about 1e-7 relative to a block's
+                       largest element): it does not meet the FP64 bar */
 };
 
 /* Unit status.  A large-grid (PSM92) quadrature that exhausts its levels keeps

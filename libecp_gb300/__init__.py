@@ -25,6 +25,7 @@ _F = ct.POINTER(ct.c_float)
 
 ECPGB_FP64 = 0   # plain FP64 kernels (the drop-in path)
 ECPGB_FAST = 1   # batched FP64 path
+ECPGB_MIXED = 2  # batched path with FP32 Bessel Taylor rows and ECP channel terms
 UNIT_DONE, UNIT_SKIPPED, UNIT_WARN_TYPE1, UNIT_WARN_TYPE2 = 0, 1, 2, 3
 
 
@@ -180,12 +181,8 @@ def get_integrals_info(s: EcpSystem, mode: int = ECPGB_FP64):
     return rc, I, info.as_dict()
 
 
-def blocks(s: EcpSystem, mode: int = ECPGB_FP64, with_status: bool = False):
-    """All emitted blocks in the reference's callback order.
-
-    Returns (meta, data) like the oracle: meta rows (A, s1, la, B, s2, lb, C,
-    type), data the blocks back to back.
-    """
+def raw_blocks(s: EcpSystem, mode: int = ECPGB_FP64):
+    """ecpgb_blocks as arrays: (values, per-unit offsets, per-unit status, info)."""
     L = lib()
     cs = c_system(s)
     nu, nv = ct.c_longlong(0), ct.c_longlong(0)
@@ -199,6 +196,17 @@ def blocks(s: EcpSystem, mode: int = ECPGB_FP64, with_status: bool = False):
                         st.ctypes.data_as(_I), ct.byref(info))
     if rc:
         raise RuntimeError(f"ecpgb_blocks failed: {last_error()}")
+    return vals[:nv.value], offs[:nu.value], st[:nu.value], info.as_dict()
+
+
+def blocks(s: EcpSystem, mode: int = ECPGB_FP64, with_status: bool = False):
+    """All emitted blocks in the reference's callback order.
+
+    Returns (meta, data) like the oracle: meta rows (A, s1, la, B, s2, lb, C,
+    type), data the blocks back to back.
+    """
+    vals, offs, st, info = raw_blocks(s, mode)
+    nu = ct.c_longlong(len(st))
     meta, data = [], []
     units = unit_table(s)
     for u in range(nu.value):
@@ -214,7 +222,7 @@ def blocks(s: EcpSystem, mode: int = ECPGB_FP64, with_status: bool = False):
     meta = np.array(meta, dtype=np.int32).reshape(-1, 8)
     data = np.concatenate(data) if data else np.zeros(0)
     if with_status:
-        return meta, data, st[:nu.value], info.as_dict()
+        return meta, data, st, info
     return meta, data
 
 

@@ -202,8 +202,12 @@ static __device__ inline double binom(const double *fac, int n, int k) {
 // `f(n)` is the integrand at abscissa index n; lower-half points count from
 // `start`, upper-half points up to `end`; a level that touches no point skips
 // the absolute error test.
+// rel > 0 (the batched mixed mode only) also accepts a level of at least 63
+// points whose error estimate is below rel times the estimate itself; rel = 0
+// is the reference's test exactly (the error estimate is never negative).
 template <class Fn>
-static __device__ bool ps93_walk(const double *w, int start, int end, double tol, Fn f, double &res) {
+static __device__ bool ps93_walk(const double *w, int start, int end, double tol, double rel, Fn f,
+                                 double &res) {
   int mid = c93_slot[0], a = c93_slot[1], b = c93_slot[2];
   double p = w[mid] * f(mid);
   double q = w[a] * f(a) + w[b] * f(b);
@@ -223,7 +227,7 @@ static __device__ bool ps93_walk(const double *w, int start, int end, double tol
     if (cnt > 0) err = 16 * fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q)) / (3 * n);
     q = (1 - j) * q + j * I;
     if (cnt == 0) continue;
-    if (err < tol) {
+    if (err < tol || (n >= 63 && err < rel * fabs(16 * q / (3 * n)))) {
       res = 16 * q / (3 * n);
       return true;
     }

@@ -66,6 +66,7 @@ struct DevJob {
   const double *besT, *besC;
   const double *besH;          // Taylor coefficients [i][l <= besHL][6] (batched path)
   const double *besA;          // large-argument polynomial [l][i], stride max(besHL + 1, 6)
+  const float *besHf;          // besH in FP32 (mixed mode)
   int besHL;
   const double *shNorm;        // spherical-harmonic normalisation [l][m], side tmDim + 1
   const double *p2s, *fac, *dfac;
@@ -87,6 +88,7 @@ struct DevJob {
   const int *order;              // units by descending estimated cost (null: natural order)
   unsigned long long *queueHead; // next queue position (persistent launch); reset per run
   int gcap;                      // type-1 step-table width cap (doubles per slot per warp)
+  int mixed;                     // 1: FP32 Bessel Taylor rows and ECP channel terms
 };
 
 // Launch configuration of the batched path (picked by the autotuner).
@@ -94,6 +96,7 @@ struct FastConfig {
   int queue = 1;   // 1: persistent CTAs pulling units from the work queue; 0: a CTA per unit
   int sorted = 1;  // 1: units by descending estimated cost; 0: the reference's order
   int gcap = 45;   // type-1 step-table width cap; smaller caps fit more CTAs per SM
+  int mixed = 0;   // set from the job's mode (ECPGB_MIXED), not tuned
 };
 
 // Shared-memory layout of the unit kernel (offsets in doubles).

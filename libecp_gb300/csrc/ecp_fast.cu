@@ -24,6 +24,13 @@ namespace ecpgb {
 
 constexpr int kWarps = kUnitThreads / 32;
 constexpr int kWalkCap = 128;  // large-grid quadratures per warp and pass
+// Mixed mode: FP32 integrands carry noise of a few 1e-8 relative, below which
+// no error estimate can fall, so a quadrature also stops once its estimated
+// error is below kMixedRel of its value -- from kMixedMinPoints points on
+// only, because the successive-difference estimates of the first levels can
+// vanish by coincidence (the FP64 modes pass rel = 0).
+constexpr double kMixedRel = 1e-6;
+constexpr int kMixedMinPoints = 63;
 
 // --------------------------------------------------------------- helpers
 
@@ -52,6 +59,21 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
     const double h = J.besselN / 16;  // integer division, as the reference
     const int index = (int)floor(z * h + 0.5);
     x = z - index / h;
+    if (J.mixed) {
+      // mixed mode: the Taylor rows in FP32 (every lane of the warp is on
+      // this branch or the large-argument one, which stays FP64)
+      const float *qf = J.besHf + (size_t)index * HL1 * 6;
+      const float xf = (float)x;
+      for (int l = 0; l <= lmax; l++) {
+        const float *q = qf + 6 * l;
+        float v = fmaf(q[5], xf, q[4]);
+        v = fmaf(v, xf, q[3]);
+        v = fmaf(v, xf, q[2]);
+        v = fmaf(v, xf, q[1]);
+        K[l * stride] = (double)fmaf(v, xf, q[0]);
+      }
+      return;
+    }
     cf = J.besH + (size_t)index * HL1 * 6;
     cs = 6;
   }
@@ -83,12 +105,28 @@ static __device__ double bessel_row(const DevJob &J, int l, double z) {
   return fma(v, dz, q[0]);
 }
 
+// One ECP term d r^n exp(-a r^2) in FP32 (mixed mode): n is an integer in
+// practice (0, 1, 2 in every basis set seen); other n take powf.
+static __device__ inline float term_f32(const DevJob &J, int t, float r, float r2) {
+  const double n = J.termN[t];
+  float p = n == 0.0 ? 1.0f : n == 1.0 ? r : n == 2.0 ? r * r : powf(r, (float)n);
+  return (float)J.termD[t] * p * expf(-(float)J.termA[t] * r2);
+}
+
 // U_l(r) of centre c for the channels l set in mask, in one pass over its
 // terms (src/ecp.c:42-60); the other entries of U are left untouched.
 static __device__ void channels_masked(const DevJob &J, int c, double r, unsigned mask, double *U) {
   double r2 = r * r;
   for (unsigned m = mask; m; m &= m - 1) U[__ffs(m) - 1] = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
+  if (J.mixed) {
+    const float rf = (float)r, r2f = (float)r2;
+    for (int t = t0; t < t1; t++) {
+      int l = J.termL[t];
+      if (mask >> l & 1u) U[l] += (double)term_f32(J, t, rf, r2f);
+    }
+    return;
+  }
   for (int t = t0; t < t1; t++) {
     int l = J.termL[t];
     if (mask >> l & 1u) U[l] += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
@@ -98,6 +136,13 @@ static __device__ void channels_masked(const DevJob &J, int c, double r, unsigne
 static __device__ double channel(const DevJob &J, int c, int l, double r) {
   double r2 = r * r, pot = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
+  if (J.mixed) {
+    const float rf = (float)r, r2f = (float)r2;
+    float pf = 0.0f;
+    for (int t = t0; t < t1; t++)
+      if (J.termL[t] == l) pf += term_f32(J, t, rf, r2f);
+    return (double)pf;
+  }
   for (int t = t0; t < t1; t++)
     if (J.termL[t] == l) pot += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
   return pot;
@@ -121,8 +166,8 @@ static __device__ inline int step_end92(int s0) { return s0 == 0 ? 31 : s0 + 32;
 // large-grid schedule; `val(pos)` = w * f at slot pos; `vis(pos)` whether the
 // (upper) point counts.  State in I, p, q; returns through done/res.
 template <class V, class Vis>
-static __device__ inline void psm92_advance(int s0, int s1, double tol, V val, Vis vis, double &I,
-                                            double &p, double &q, bool &done, double &res) {
+static __device__ inline void psm92_advance(int s0, int s1, double tol, double rel, V val, Vis vis,
+                                            double &I, double &p, double &q, bool &done, double &res) {
   int pos = s0;
   if (pos == 0) {
     I = val(0);
@@ -143,7 +188,10 @@ static __device__ inline void psm92_advance(int s0, int s1, double tol, V val, V
     pos += 2;
     if (pos == c92_lvEnd[k]) {
       double N = c92_lvN[k] + 1.0, e = I - p;
-      if (16 * e * e <= 3 * N * fabs(I - q) * tol) {
+      // mixed mode: the reference's two-difference test with the tolerance
+      // raised to rel times the estimate
+      const double t = N >= kMixedMinPoints ? fmax(tol, rel * fabs(16 * I / (3 * N))) : tol;
+      if (16 * e * e <= 3 * N * fabs(I - q) * t) {
         res = 16 * I / (3 * N);
         done = true;
       }
@@ -292,6 +340,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
                                     const double *pcA, const double *pzB, const double *pcB,
                                     const double *gA, const double *gB, int ws, int we, int &warn) {
   const int lane = threadIdx.x & 31, lab = la + lb, lq = lab + 1, O = kSmallOrder;
+  const double rel = J.mixed ? kMixedRel : 0.0;
   // odd entry strides: lanes touching neighbouring entries hit distinct banks
   const int OL = J.largeOrder, TSs = 1 + 2 * lq, TSf = 3 + 2 * lq, RQ = lq * lq, nq = t1_items(lab);
   double *sc = W + L.w1Sc, *rsh = W + L.w1Rsh, *Q = W + L.w1Q, *H = W + L.w1H, *tab = W + L.w1Tab;
@@ -378,7 +427,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
           p += (1 - j) * (I - q);
           if (cnt > 0) err = 16 * fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q)) / (3 * n);
           q = (1 - j) * q + j * I;
-          if (cnt > 0 && err < J.tol) {
+          if (cnt > 0 && (err < J.tol || (n >= kMixedMinPoints && err < rel * fabs(16 * q / (3 * n))))) {
             done = true;
             Q[g * RQ + l1 * lq + l2] += 16 * q / (3 * n);
           }
@@ -459,7 +508,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
           return e[1] == 0.0 ? 0.0 : e[0] * (e[1] * e[2 + lq + l1] * e[2 + l2]);
         };
         auto vis = [&](int t) { return c92_slot[t] <= end; };
-        psm92_advance(s0, s1, J.tol, val, vis, I2, p2, q2, done2, res2);
+        psm92_advance(s0, s1, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I2, p2, q2, done2, res2);
       }
       __syncwarp();
       s0 = s1;
@@ -573,7 +622,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       auto vis = [&](int t) { return tab[(t - s0) * TS + 2] != 0.0; };
       double I = sI[q], p = sP[q], qv = sQ[q], res = 0;
       bool done = false;
-      psm92_advance(s0, s1, J.tol, val, vis, I, p, qv, done, res);
+      psm92_advance(s0, s1, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
       sI[q] = I; sP[q] = p; sQ[q] = qv;
       if (done) { sR[q] = res; doneBits[qi] |= 1u << lane; }
       else all = false;
@@ -720,7 +769,8 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     item(q, l, l1, l2, l3);
     const int nk = J.nk;
     double res;
-    bool ok = ps93_walk(J.wSmall, ws, we, J.tol,
+    // FP64 integrand in every mode: the reference's test
+    bool ok = ps93_walk(J.wSmall, ws, we, J.tol, 0.0,
                         [&](int n) {
                           return Fa[n * nF + l1] * Fb[n * nF + l2] * Ut[((size_t)n * LE + l) * nk + l3];
                         },
@@ -911,6 +961,7 @@ int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, con
   if (smemBytes > 200 * 1024) return 3;
   DevJob Jc = J;
   Jc.gcap = cfg.gcap;
+  Jc.mixed = cfg.mixed;
   if (!cfg.sorted) Jc.order = nullptr;
   launch_prologue(Jc, st);
   long long nUnits = (long long)J.nCentres * J.nPairs;

@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
       while (rem >= l1 / 2 + 1) { rem -= l1 / 2 + 1; l1++; }
       int l2 = l1 - 2 * rem;
       double res;
-      bool ok = ps93_walk(J.wSmall, ws, we, tol,
+      bool ok = ps93_walk(J.wSmall, ws, we, tol, 0.0,
                           [&](int n) { return C1 * R1[n * nA + l1] * U1[n] * K1[n * nA + l2] * EX1[n]; },
                           res);
       if (ok) Q[l1 * (lab + 1) + l2] += res;
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
     item(q, l, l1, l2, l3);
     const int nk = J.nk;
     double res;
-    bool ok = ps93_walk(J.wSmall, ws, we, tol,
+    bool ok = ps93_walk(J.wSmall, ws, we, tol, 0.0,
                         [&](int n) {
                           return Fa[n * nF + l1] * Fb[n * nF + l2] * Ut[((size_t)n * LE + l) * nk + l3];
                         },

@@ -146,6 +146,7 @@ int parse_system(const ecpgb_system &s, Parsed &P) {
 struct DevTables {
   TableKey key{};
   HostTables host;
+  DBuf<float> besHf;
   DBuf<double> xs, ws, xl, wl, besT, besC, besH, besA, shNorm, p2s, fac, dfac, omega;
   DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items;
   int nItemsMax = 0;
@@ -204,7 +205,7 @@ struct Engine {
               t->besC.upload(h.besselC, stream) && t->p2s.upload(h.poly2sph, stream) &&
               t->fac.upload(h.fac, stream) && t->dfac.upload(h.dfac, stream) &&
               t->omega.upload(h.omega, stream) && t->ijk.upload(h.ijk, stream) &&
-              t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) && t->besA.upload(h.besselA, stream) &&
+              t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) && t->besA.upload(h.besselA, stream) && t->besHf.upload(h.besselHf, stream) &&
               t->shNorm.upload(h.shNorm, stream);
     // used-triple lists per (la, lb, l)
     int LB = h.maxLBS, LE = h.maxLECP > 0 ? h.maxLECP : 1;
@@ -309,6 +310,8 @@ void wait_schedules_unpinned(std::unique_lock<std::mutex> &lk) {
 
 static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 
+bool valid_mode(int mode) { return mode == ECPGB_FP64 || mode == ECPGB_FAST || mode == ECPGB_MIXED; }
+
 // The work queue of the batched path: units by descending estimated cost,
 // primitive pairs x (la + lb + 2) x (L + 2), ties in the reference's order
 // (a stable counting sort).  Empty when the units do not fit 31-bit indices.
@@ -352,7 +355,7 @@ size_t job_device_bytes(const Parsed &P, int mode) {
   const size_t angLam = P.maxLECP + LB + 1, angC = (LB + 1) * (LB + 2) * (LB + 3) / 6;
   size_t in = 8 * (P.geom.size() + P.primA.size() + P.primD.size() + 3 * P.termL.size() + P.pairOff.size()) +
               4 * (5 * P.shL.size() + P.atomMaxL.size() + 4 * P.ctrAtom.size() + P.termL.size() + 2 * P.pairA.size()) +
-              (mode == ECPGB_FAST ? 4 * nc * P.nPairs : 0) + 21 * 256;
+              (mode != ECPGB_FP64 ? 4 * nc * P.nPairs : 0) + 21 * 256;
   size_t work = 8 * (ns + nc * O * LE * nk + nc * O + nc * ns * O * nF + nc * na * 4 + nc * na * D * D * D +
                      nc * na * angLam * LE * LE * angC + nc * (size_t)P.centreStride + (size_t)P.dim * P.dim) +
                 4 * (nc + nc * ns * 3 + nc * (size_t)P.nPairs + 2) + 8;
@@ -395,7 +398,7 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
          iTL = add(P.termL.data(), 4 * P.termL.size()), iPrA = add(P.pairA.data(), 4 * P.pairA.size()),
          iPrB = add(P.pairB.data(), 4 * P.pairB.size()), iPO = add(P.pairOff.data(), 8 * P.pairOff.size());
   std::vector<int> order;
-  if (mode == ECPGB_FAST) unit_order(P, order);
+  if (mode != ECPGB_FP64) unit_order(P, order);
   size_t iOrd = add(order.data(), 4 * order.size());
   if (!B.pinned.ensure(tot) || !B.in.ensure(tot)) {
     set_error("allocation of %zu input bytes failed", tot);
@@ -438,6 +441,8 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.gcap = FastConfig{}.gcap;
   J.besH = T->besH.p;
   J.besA = T->besA.p;
+  J.besHf = T->besHf.p;
+  J.mixed = mode == ECPGB_MIXED;
   J.besHL = h.besselHL;
   J.shNorm = T->shNorm.p;
   UnitSmem L = unit_smem_layout(h.maxLBS, h.maxLECP, h.nF);
@@ -452,8 +457,9 @@ int run_pipeline(JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0, cudaE
   launch_reset(J, stream);
   CUDA_OK(cudaMemsetAsync(B.mat.p, 0, sizeof(double) * (size_t)J.dim * J.dim, stream));
   int rc;
-  if (mode == ECPGB_FAST) {
-    const FastConfig c = cfg ? *cfg : engine().config_for(J.maxLBS, J.maxLECP);
+  if (mode == ECPGB_FAST || mode == ECPGB_MIXED) {
+    FastConfig c = cfg ? *cfg : engine().config_for(J.maxLBS, J.maxLECP);
+    c.mixed = mode == ECPGB_MIXED;
     rc = launch_fast_pipeline(J, stream, fast_smem_bytes(J.maxLBS, J.maxLECP, J.nF, c.gcap), c, u0, u1);
   } else {
     rc = launch_fp64_pipeline(J, stream, B.smem, u0, u1);
@@ -471,7 +477,7 @@ int run_pipeline(JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0, cudaE
 int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_info *info) {
   Engine &E = engine();
   std::unique_lock<std::mutex> lk(E.mu);
-  if (mode != ECPGB_FP64 && mode != ECPGB_FAST) { set_error("unknown mode %d", mode); return 1; }
+  if (!valid_mode(mode)) { set_error("unknown mode %d", mode); return 1; }
   if (E.ensure_init()) return 1;
   Parsed P;
   if (parse_system(s, P)) return 1;
@@ -522,7 +528,7 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
                ecpgb_info *info, Parsed *parsedOut) {
   Engine &E = engine();
   std::unique_lock<std::mutex> lk(E.mu);
-  if (mode != ECPGB_FP64 && mode != ECPGB_FAST) { set_error("unknown mode %d", mode); return 1; }
+  if (!valid_mode(mode)) { set_error("unknown mode %d", mode); return 1; }
   if (E.ensure_init()) return 1;
   Parsed P;
   if (parse_system(s, P)) return 1;
@@ -614,7 +620,7 @@ static int capture_graph(Engine &E, ResidentJob *R) {
   if (R->graph) return 0;
   if (!R->gu0) cudaEventCreate(&R->gu0);
   if (!R->gu1) cudaEventCreate(&R->gu1);
-  if (R->mode == ECPGB_FAST) fast_prepare();  // function attributes before capture
+  if (R->mode != ECPGB_FP64) fast_prepare();  // function attributes before capture
   cudaGraph_t g = nullptr;
   CUDA_OK(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
   int rc = run_pipeline(R->B, R->J, R->mode, R->gu0, R->gu1, &R->cfg, E.stream);
@@ -637,7 +643,7 @@ static int capture_graph(Engine &E, ResidentJob *R) {
 void *job_create(const ecpgb_system &s, int mode) {
   Engine &E = engine();
   std::lock_guard<std::mutex> lk(E.mu);
-  if (mode != ECPGB_FP64 && mode != ECPGB_FAST) { set_error("unknown mode %d", mode); return nullptr; }
+  if (!valid_mode(mode)) { set_error("unknown mode %d", mode); return nullptr; }
   if (E.ensure_init()) return nullptr;
   auto *R = new ResidentJob();
   R->mode = mode;
@@ -716,7 +722,7 @@ int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials,
   std::unique_lock<std::mutex> lk(E.mu);
   auto *R = (ResidentJob *)vj;
   if (nTrials) *nTrials = 0;
-  if (R->mode != ECPGB_FAST) { set_error("the autotuner applies to the batched path only"); return 3; }
+  if (R->mode == ECPGB_FP64) { set_error("the autotuner applies to the batched path only"); return 3; }
   if (E.use_schedules(R->T, &lk)) return 1;
   // candidates: queue or CTA-per-unit, cost order or the reference's, and
   // the step-table cap (pairs per warp against CTAs per SM)
@@ -769,7 +775,7 @@ int job_config(void *vj, const ecpgb_launch_config *cfg, ecpgb_launch_config *ou
   std::lock_guard<std::mutex> lk(E.mu);
   auto *R = (ResidentJob *)vj;
   if (cfg) {
-    if (R->mode != ECPGB_FAST) { set_error("launch configurations apply to the batched path only"); return 3; }
+    if (R->mode == ECPGB_FP64) { set_error("launch configurations apply to the batched path only"); return 3; }
     if (cfg->gcap < 1 || cfg->gcap > 4096) { set_error("gcap %d out of range", cfg->gcap); return 1; }
     FastConfig c{cfg->queue ? 1 : 0, cfg->sorted ? 1 : 0, cfg->gcap};
     if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap), c.queue) < 1) {

@@ -125,6 +125,8 @@ void schedules_overwritten();
 void wait_schedules_unpinned(std::unique_lock<std::mutex> &lk);
 int run_matrix_noalloc(const ecpgb_system &s, int rowdim, double *I);
 
+bool valid_mode(int mode);
+
 // ---- internals shared with the request server (ecp_serve.cpp)
 struct DevTables;
 // Packs P's inputs into B's pinned buffer, copies them to the device on

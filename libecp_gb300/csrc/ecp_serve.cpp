@@ -223,7 +223,7 @@ struct Server {
 }  // namespace
 
 void *server_create(int mode, long long budget, int nSlots) {
-  if (mode != ECPGB_FP64 && mode != ECPGB_FAST) {
+  if (!valid_mode(mode)) {
     set_error("unknown mode %d", mode);
     return nullptr;
   }

@@ -408,6 +408,7 @@ void bessel_horner(HostTables &t) {
       for (int l = 0; l <= HL; l++) c[l * 6 + k] = d[l] * invfact[k];
     }
   }
+  t.besselHf.assign(t.besselH.begin(), t.besselH.end());
   const int AS = HL + 1 < 6 ? 6 : HL + 1;
   t.besselA.assign((size_t)(HL + 1) * AS, 0.0);
   for (int l = 0; l <= HL; l++) {
