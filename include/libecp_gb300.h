@@ -105,10 +105,12 @@ void ecpgb_job_free(ecpgb_job *j);
  * unit; sorted: 1 = the queue holds the units by descending estimated cost
  * (primitive pairs x (la + lb + 2) x (L + 2)), 0 = the reference's order;
  * gcap: width cap of the type-1 step table in doubles per slot, which sets
- * the primitive pairs per warp and the CTAs per SM.  msUnit: the unit
- * kernel's time when the autotuner measured it, else 0. */
+ * the primitive pairs per warp and the CTAs per SM; balance: 1 = a unit with
+ * few primitive pairs gets narrower type-1 groups so that all its warps
+ * work.  msUnit: the unit kernel's time when the autotuner measured it, else
+ * 0. */
 typedef struct {
-  int queue, sorted, gcap;
+  int queue, sorted, gcap, balance;
   float msUnit;
 } ecpgb_launch_config;
 
@@ -117,8 +119,9 @@ typedef struct {
  * for later jobs of the same (max basis l, max ECP L) in this process, and
  * reports it in *chosen.  trials (may be NULL) receives up to maxTrials
  * candidates with their times; *nTrials the number written.  queue and sorted
- * leave every result bit for bit unchanged; gcap regroups the primitive pairs
- * of the type-1 sums over warps, which moves results at rounding level only.
+ * leave every result bit for bit unchanged; gcap and balance regroup the
+ * primitive pairs of the type-1 sums over warps, which moves results at
+ * rounding level only.
  * 0 ok, 1 error, 3 the job is not a batched-path job. */
 int ecpgb_job_tune(ecpgb_job *j, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials,
                    int *nTrials);

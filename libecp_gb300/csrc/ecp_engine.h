@@ -89,6 +89,7 @@ struct DevJob {
   unsigned long long *queueHead; // next queue position (persistent launch); reset per run
   int gcap;                      // type-1 step-table width cap (doubles per slot per warp)
   int mixed;                     // 1: FP32 Bessel Taylor rows and ECP channel terms
+  int balance;                   // 1: type-1 groups narrowed so that every warp gets pairs
 };
 
 // Launch configuration of the batched path (picked by the autotuner).
@@ -97,6 +98,7 @@ struct FastConfig {
   int sorted = 1;  // 1: units by descending estimated cost; 0: the reference's order
   int gcap = 45;   // type-1 step-table width cap; smaller caps fit more CTAs per SM
   int mixed = 0;   // set from the job's mode (ECPGB_MIXED), not tuned
+  int balance = 1; // narrower type-1 groups when a unit has few primitive pairs
 };
 
 // Shared-memory layout of the unit kernel (offsets in doubles).

@@ -681,7 +681,12 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     const int ncab = (lab + 1) * (lab + 2) * (lab + 3) / 6;
     for (int e = tid & 31; e < ncab; e += 32) W[Lm.w1H + e] = 0.0;
     __syncwarp();
-    const int G = t1_group(lab, J.gcap);
+    int G = t1_group(lab, J.gcap);
+    // balance: with few primitive pairs, narrower groups keep all warps busy
+    if (J.balance) {
+      const int Gb = (NP + kWarps - 1) / kWarps;
+      if (Gb < G) G = Gb > 0 ? Gb : 1;
+    }
     for (int p0 = warp * G; p0 < NP; p0 += kWarps * G)
       t1_group_run(J, Lm, W, c, Lc, la, lb, p0, NP - p0 < G ? NP - p0 : G, Nb, pzA, pcA, pzB, pcB, gA, gB,
                    ws, we, warn1);
@@ -962,6 +967,7 @@ int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, con
   DevJob Jc = J;
   Jc.gcap = cfg.gcap;
   Jc.mixed = cfg.mixed;
+  Jc.balance = cfg.balance;
   if (!cfg.sorted) Jc.order = nullptr;
   launch_prologue(Jc, st);
   long long nUnits = (long long)J.nCentres * J.nPairs;

@@ -715,7 +715,7 @@ int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
   return 0;
 }
 
-static ecpgb_launch_config to_c(const FastConfig &c, float ms) { return {c.queue, c.sorted, c.gcap, ms}; }
+static ecpgb_launch_config to_c(const FastConfig &c, float ms) { return {c.queue, c.sorted, c.gcap, c.balance, ms}; }
 
 int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials, int *nTrials) {
   Engine &E = engine();
@@ -727,9 +727,18 @@ int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials,
   // candidates: queue or CTA-per-unit, cost order or the reference's, and
   // the step-table cap (pairs per warp against CTAs per SM)
   std::vector<FastConfig> cand;
+  auto mk = [](int queue, int sorted, int gcap, int balance) {
+    FastConfig c;
+    c.queue = queue;
+    c.sorted = sorted;
+    c.gcap = gcap;
+    c.balance = balance;
+    return c;
+  };
   for (int gcap : {45, 64, 33})
-    for (int queue : {1, 0}) cand.push_back(FastConfig{queue, 1, gcap});
-  cand.push_back(FastConfig{0, 0, 45});
+    for (int queue : {1, 0}) cand.push_back(mk(queue, 1, gcap, 1));
+  cand.push_back(mk(0, 0, 45, 1));
+  cand.push_back(mk(1, 1, 45, 0));
   const size_t flushBytes = 256u << 20;
   if (!E.flush.ensure(flushBytes)) { set_error("flush buffer allocation failed"); return 1; }
   cudaEvent_t u0, u1;
@@ -777,7 +786,11 @@ int job_config(void *vj, const ecpgb_launch_config *cfg, ecpgb_launch_config *ou
   if (cfg) {
     if (R->mode == ECPGB_FP64) { set_error("launch configurations apply to the batched path only"); return 3; }
     if (cfg->gcap < 1 || cfg->gcap > 4096) { set_error("gcap %d out of range", cfg->gcap); return 1; }
-    FastConfig c{cfg->queue ? 1 : 0, cfg->sorted ? 1 : 0, cfg->gcap};
+    FastConfig c;
+    c.queue = cfg->queue ? 1 : 0;
+    c.sorted = cfg->sorted ? 1 : 0;
+    c.gcap = cfg->gcap;
+    c.balance = cfg->balance ? 1 : 0;
     if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap), c.queue) < 1) {
       set_error("configuration does not fit on an SM");
       return 1;

@@ -55,8 +55,8 @@ def test_every_config_within_parity_of_fp64(eg, system):
     ref_v, ref_s = _run(eg, jp)
     jp.close()
     j = eg.Job(system, mode=eg.ECPGB_FAST)
-    for gcap in (33, 45, 64):
-        v, s = _run(eg, j, queue=1, sorted=1, gcap=gcap)
+    for gcap, balance in ((33, 1), (45, 1), (64, 1), (45, 0)):
+        v, s = _run(eg, j, queue=1, sorted=1, gcap=gcap, balance=balance)
         assert np.array_equal(s, ref_s), gcap
         err = np.abs(v - ref_v).max()  # skipped units read zero in both
         assert err <= TOL_ABS, (gcap, err)
@@ -69,9 +69,10 @@ def test_autotuner_picks_a_measured_candidate(eg, system):
     assert len(trials) >= 4
     assert all(t["msUnit"] > 0 for t in trials)
     best = min(trials, key=lambda t: t["msUnit"])
-    assert (chosen["queue"], chosen["sorted"], chosen["gcap"]) == (best["queue"], best["sorted"], best["gcap"])
+    key = ("queue", "sorted", "gcap", "balance")
+    assert tuple(chosen[k] for k in key) == tuple(best[k] for k in key)
     cur = j.config()
-    assert (cur["queue"], cur["sorted"], cur["gcap"]) == (chosen["queue"], chosen["sorted"], chosen["gcap"])
+    assert tuple(cur[k] for k in key) == tuple(chosen[k] for k in key)
     # the tuned job still matches the drop-in matrix path
     ms, _ = j.run(1)
     I1 = j.matrix()
