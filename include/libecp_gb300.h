@@ -29,6 +29,15 @@ typedef struct {
   const double *dBS, *aBS;
   int largeGridOrder;
   double tolerance, accuracy;
+  /* nuclear-derivative order n of libECP_init (src/libecp.h:15-21): 0, 1 or
+   * 2.  With n > 0 every (shell pair, centre) carries the shifted blocks of
+   * the reference's derivative scheme (src/libecp.c:240-248): (shifta,
+   * shiftb) from {(0,0)} for n = 0, {(+1,0),(-1,0),(0,+1),(0,-1)} for n = 1,
+   * {(+2,0),(-2,0),(+1,+1),(+1,-1),(-1,+1),(-1,-1),(0,+2),(0,-2),(+1,0),
+   * (0,+1)} for n = 2, each a type-1 and a type-2 block of the shifted
+   * Cartesian shells with coefficients times zeta^max(0, shift).  The AO
+   * matrix (getIntegrals, ecpgb_getIntegrals) exists for n = 0 only. */
+  int derivative;
 } ecpgb_system;
 
 enum {

@@ -33,7 +33,7 @@ class EcpgbSystem(ct.Structure):
     _fields_ = [("nrAtoms", ct.c_int), ("geometry", _D), ("shellsECP", _I), ("KECP", _I),
                 ("lECP", _I), ("nECP", _D), ("dECP", _D), ("aECP", _D), ("shellsBS", _I),
                 ("lBS", _I), ("KBS", _I), ("dBS", _D), ("aBS", _D), ("largeGridOrder", ct.c_int),
-                ("tolerance", ct.c_double), ("accuracy", ct.c_double)]
+                ("tolerance", ct.c_double), ("accuracy", ct.c_double), ("derivative", ct.c_int)]
 
 
 class EcpgbInfo(ct.Structure):
@@ -158,7 +158,7 @@ def _ptrs(s: EcpSystem):
 def c_system(s: EcpSystem) -> EcpgbSystem:
     p = _ptrs(s)
     return EcpgbSystem(p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[10], p[11],
-                       p[12], p[13], p[14], p[15])
+                       p[12], p[13], p[14], p[15], int(getattr(s, "derivative", 0)))
 
 
 def get_integrals(s: EcpSystem, I: np.ndarray | None = None) -> np.ndarray:
@@ -227,6 +227,48 @@ def blocks(s: EcpSystem, mode: int = ECPGB_FP64, with_status: bool = False):
     return meta, data
 
 
+# Derivative shifts of libECP_init's order n (src/libecp.c:240-248).
+SHIFTS = {0: [(0, 0)],
+          1: [(1, 0), (-1, 0), (0, 1), (0, -1)],
+          2: [(2, 0), (-2, 0), (1, 1), (1, -1), (-1, 1), (-1, -1), (0, 2), (0, -2), (1, 0), (0, 1)]}
+
+
+def block_l(n: int, la: int, lb: int, ha: int, hb: int):
+    """l of the blocks a shifted unit hands out (src/libecp.c:356-362)."""
+    lpa, lpb = la + ha, lb + hb
+    if n == 2 and (ha, hb) == (1, 0):
+        lpa = la
+    elif n == 2 and (ha, hb) == (0, 1):
+        lpb = lb
+    return lpa, lpb
+
+
+def blocks_deriv(s: EcpSystem, mode: int = ECPGB_FP64, with_status: bool = False):
+    """Derivative blocks (s.derivative = 1 or 2) in the reference's callback
+    order: meta rows (A, s1, la, shifta, B, s2, lb, shiftb, C, type), data."""
+    n = int(s.derivative)
+    vals, offs, st, info = raw_blocks(s, mode)
+    base = unit_table(s)  # (A, s1, la, B, s2, lb, C) per (centre, pair)
+    shifts = SHIFTS[n]
+    meta, data = [], []
+    for i, (A, s1, la, B, s2, lb, C) in enumerate(base):
+        for k, (ha, hb) in enumerate(shifts):
+            u = i * len(shifts) + k
+            if st[u] == UNIT_SKIPPED:
+                continue
+            lpa, lpb = block_l(n, la, lb, ha, hb)
+            m = ncart(lpa) * ncart(lpb)
+            o = int(offs[u])
+            for t in (1, 2):
+                meta.append((A, s1, la, ha, B, s2, lb, hb, C, t))
+                data.append(vals[o + (t - 1) * m:o + t * m])
+    meta = np.array(meta, dtype=np.int32).reshape(-1, 10)
+    data = np.concatenate(data) if data else np.zeros(0)
+    if with_status:
+        return meta, data, st, info
+    return meta, data
+
+
 def unit_table(s: EcpSystem):
     """(A, s1, la, B, s2, lb, C) per unit u = centre_rank * nPairs + pair."""
     shells = []
@@ -249,31 +291,38 @@ def unit_table(s: EcpSystem):
 
 def calculate_blocks_via_callback(s: EcpSystem):
     """Drives libECP_init / calculateECPIntegrals / libECP_free and records the
-    callback stream: (status, meta, data) in callback order."""
+    callback stream: (status, meta, data) in callback order.  Meta rows are
+    (A, s1, la, B, s2, lb, C, type) for derivative order 0 and
+    (A, s1, la, shifta, B, s2, lb, shiftb, C, type) otherwise."""
     L = lib()
     p = _ptrs(s)
+    n = int(getattr(s, "derivative", 0))
     # libECP_init reads (shellsECP, lECP, KECP) -- the definition's order
     h = L.libECP_init(p[0], p[1], p[2], p[4], p[3], p[5], p[6], p[7], p[8], p[9], p[10], p[11],
-                      p[12], 0, -1, None, p[13], p[14], p[15])
+                      p[12], n, -1, None, p[13], p[14], p[15])
     if not h:
         raise RuntimeError(f"libECP_init failed: {last_error()}")
     meta, data = [], []
     last = {"key": None, "type": 0}
 
     def cb(A, sa, la, shifta, B, sb, lb, shiftb, C, I, _p):
-        key = (A, sa, B, sb, C)
+        key = (A, sa, B, sb, C, shifta, shiftb)
         t = 2 if (last["key"] == key and last["type"] == 1) else 1
         last["key"], last["type"] = key, t
-        n = ncart(la) * ncart(lb)
-        meta.append((A, sa, la, B, sb, lb, C, t))
-        data.append(np.ctypeslib.as_array(I, shape=(n,)).copy())
+        lpa, lpb = block_l(n, la, lb, shifta, shiftb)
+        m = ncart(lpa) * ncart(lpb)
+        if n:
+            meta.append((A, sa, la, shifta, B, sb, lb, shiftb, C, t))
+        else:
+            meta.append((A, sa, la, B, sb, lb, C, t))
+        data.append(np.ctypeslib.as_array(I, shape=(m,)).copy())
 
     c_cb = ECP_CALLBACK(cb)
     try:
         rc = L.calculateECPIntegrals(h, c_cb, None)
     finally:
         L.libECP_free(h)
-    meta = np.array(meta, dtype=np.int32).reshape(-1, 8)
+    meta = np.array(meta, dtype=np.int32).reshape(-1, 10 if n else 8)
     return rc, meta, (np.concatenate(data) if data else np.zeros(0))
 
 

@@ -56,8 +56,8 @@ libECPHandle *libECP_init(int nrAtoms, double *geometry, int *shellsECP, int *lE
                           int *KBS, double *dBS, double *aBS, int n, int lmax, int *shellOrdering,
                           int largeGridOrder, double tolerance, double accuracy) {
   (void)lmax;
-  if (n != 0) {
-    ecpgb::set_error("derivative order %d: only n = 0 is implemented", n);
+  if (n < 0 || n > 2) {  // the reference's shift table covers orders 0..2 (src/libecp.c:243-248)
+    ecpgb::set_error("derivative order %d outside 0..2", n);
     return nullptr;
   }
   if (shellOrdering != nullptr) {
@@ -77,14 +77,14 @@ libECPHandle *libECP_init(int nrAtoms, double *geometry, int *shellsECP, int *lE
   h->aECP.assign(aECP, aECP + nt);
   h->sys = {nrAtoms, geometry, h->shellsECP.data(), h->KECP.data(), h->lECP.data(), h->nECP.data(),
             h->dECP.data(), h->aECP.data(), shellsBS, lBS, KBS, dBS, aBS, largeGridOrder,
-            tolerance, accuracy};
+            tolerance, accuracy, n};
   ecpgb::Parsed P;
   if (ecpgb::parse_system(h->sys, P)) {
     delete h;
     return nullptr;
   }
   ecpgb::HostTables t;
-  ecpgb::build_tables({P.maxLECP, P.maxLBS, largeGridOrder, tolerance, accuracy}, t);
+  ecpgb::build_tables(ecpgb::table_key(P), t);
   if (t.status) {  // e.g. the Bessel series does not converge (src/libecp.c:181-185)
     delete h;
     return nullptr;
@@ -112,12 +112,17 @@ int calculateECPIntegrals(libECPHandle *h, ECPCallback cb, void *args) {
     int c = (int)(u / P.nPairs), p = (int)(u % P.nPairs);
     int sa = P.pairA[p], sb = P.pairB[p], la = P.shL[sa], lb = P.shL[sb];
     int A = P.shAtom[sa], B = P.shAtom[sb], C = P.ctrAtom[c];
-    size_t nb = (size_t)ncart(la) * ncart(lb);
+    int ha = 0, hb = 0, lpa = la, lpb = lb;  // derivative shift and the blocks' l
+    if (P.deriv) {
+      ecpgb::shift_pair(P.deriv, P.pairShift[p], ha, hb);
+      ecpgb::shift_block_l(P.deriv, la, lb, ha, hb, lpa, lpb);
+    }
+    size_t nb = (size_t)ncart(lpa) * ncart(lpb);
     const double *b1 = values.data() + offsets[u];
     blk.assign(b1, b1 + nb);
-    cb(A, P.shLocal[sa], la, 0, B, P.shLocal[sb], lb, 0, C, blk.data(), args);
+    cb(A, P.shLocal[sa], la, ha, B, P.shLocal[sb], lb, hb, C, blk.data(), args);
     blk.assign(b1 + nb, b1 + 2 * nb);
-    cb(A, P.shLocal[sa], la, 0, B, P.shLocal[sb], lb, 0, C, blk.data(), args);
+    cb(A, P.shLocal[sa], la, ha, B, P.shLocal[sb], lb, hb, C, blk.data(), args);
     if (result == 0 && st == ECPGB_UNIT_WARN_TYPE1) result = 1;
     if (result == 0 && st == ECPGB_UNIT_WARN_TYPE2) result = 2;
   }

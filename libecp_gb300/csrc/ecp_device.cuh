@@ -75,6 +75,42 @@ static __device__ void bessel_eval(const DevJob &J, int lmax, double z, double *
   }
 }
 
+// Derivative shifts (src/libecp.c:240-248), indexed [order][shift].
+static __constant__ int c_shiftA[3][10] = {{0}, {+1, -1, 0, 0}, {+2, -2, +1, +1, -1, -1, 0, 0, +1, 0}};
+static __constant__ int c_shiftB[3][10] = {{0}, {0, 0, +1, -1}, {0, 0, +1, -1, +1, -1, +2, -2, 0, +1}};
+
+// c times z, n times in a row: the reference's zeta^n derivative factors
+// (src/type1.c:239-246, src/type2.c:459-462); n <= 0 leaves c.
+static __device__ inline double zeta_times(double c, double z, int n) {
+  for (int k = 0; k < n; k++) c *= z;
+  return c;
+}
+
+// The derivative shift of pair entry pr and whether the reference computes
+// that (shift, centre) combination at all (src/libecp.c:296-330):
+// la, lb are the shells' l; A, B their atoms; C the centre's atom.
+struct UnitShift {
+  int a, b;       // shifta, shiftb
+  int lpa, lpb;   // l of the blocks handed out
+  bool skip;
+};
+static __device__ inline UnitShift unit_shift(const DevJob &J, int pr, int la, int lb, int A, int B, int C) {
+  UnitShift s{0, 0, la, lb, false};
+  if (!J.pairShift || J.deriv <= 0) return s;
+  const int k = J.pairShift[pr], d = J.deriv;
+  s.a = c_shiftA[d][k];
+  s.b = c_shiftB[d][k];
+  s.lpa = la + s.a;
+  s.lpb = lb + s.b;
+  if (d == 2) {  // src/libecp.c:356-362
+    if (s.a == 1 && s.b == 0) s.lpa = la;
+    else if (s.a == 0 && s.b == 1) s.lpb = lb;
+  }
+  s.skip = (A == C && B == C) || la + s.a < 0 || lb + s.b < 0 || (d == 1 && C == A && s.a != 0) ||
+           (d == 1 && C == B && s.b != 0);
+  return s;
+}
+
 // r^n for the ECP exponent n (a double in the interface; integers are the norm).
 static __device__ inline double rpow(double r, double n) {
   if (n == 0.0) return 1.0;

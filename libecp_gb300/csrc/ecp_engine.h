@@ -57,6 +57,8 @@ struct DevJob {
   const int *termL;
   const double *termN, *termD, *termA;
   const int *pairA, *pairB;
+  const int *pairShift;        // derivative shift index of each pair entry (null: none)
+  int deriv, nRuns;            // derivative order; F-table runs (1 + order; 0 reads as 1)
   const long long *pairOff;    // value offset of the pair's two blocks within a centre
   long long centreStride;      // values per centre
   // used-triple lists of the type-2 angular linking, per (la, lb, l)

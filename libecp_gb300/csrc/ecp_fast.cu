@@ -338,7 +338,8 @@ static __device__ void rsh_column(const DevJob &J, int lmax, int m, double theta
 static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *W, int c, int Lc,
                                     int la, int lb, int p0, int G, int Nb, const double *pzA,
                                     const double *pcA, const double *pzB, const double *pcB,
-                                    const double *gA, const double *gB, int ws, int we, int &warn) {
+                                    const double *gA, const double *gB, int ws, int we, int pa0, int pb0,
+                                    int &warn) {
   const int lane = threadIdx.x & 31, lab = la + lb, lq = lab + 1, O = kSmallOrder;
   const double rel = J.mixed ? kMixedRel : 0.0;
   // odd entry strides: lanes touching neighbouring entries hit distinct banks
@@ -349,7 +350,9 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
   // (1) per pair: k-vector, its spherical coordinates, the prefactor
   if (lane < G) {
     int k = p0 + lane;
-    double za = pzA[k / Nb], ca = pcA[k / Nb], zb = pzB[k % Nb], cb = pcB[k % Nb];
+    // derivative blocks: coefficients times zeta^max(0, shift) (src/type1.c:239-246)
+    double za = pzA[k / Nb], ca = zeta_times(pcA[k / Nb], za, pa0), zb = pzB[k % Nb],
+           cb = zeta_times(pcB[k % Nb], zb, pb0);
     double P[3], Sp[3];
     for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * gA[i] + zb * gB[i]);
     to_spherical(P, Sp);
@@ -446,7 +449,8 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     const bool fail = failed && g == gg;
     if (!__ballot_sync(0xffffffffu, fail)) continue;
     const int kk = p0 + gg;
-    const double za = pzA[kk / Nb], ca = pcA[kk / Nb], zb = pzB[kk % Nb], cb = pcB[kk % Nb];
+    const double za = pzA[kk / Nb], ca = zeta_times(pcA[kk / Nb], za, pa0), zb = pzB[kk % Nb],
+                 cb = zeta_times(pcB[kk % Nb], zb, pb0);
     const double s = sc[gg * 6], z = -za - zb, zd2 = -za * dAC * dAC - zb * dBC * dBC;
     const double C2 = ca * cb;
     double i1, i2;
@@ -554,14 +558,16 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
 static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, const FastShared &S,
                                int k, int Nb, int nf, int c, int Lc, int la, int lb, const double *pzA,
                                const double *pcA, const double *pzB, const double *pcB, double dAC,
-                               double dBC, int ncls, int &warn) {
+                               double dBC, int ncls, int pa0, int pb0, int &warn) {
   const int lane = threadIdx.x & 31, nA = 2 * J.maxLBS + 1;
   const int LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE, OL = J.largeOrder;
   const int TS = L.tab2Stride;
   double *tab = W + L.w2Tab, *sI = W + L.w2I, *sP = W + L.w2P, *sQ = W + L.w2Q, *sR = W + L.w2R;
   double *part = W + L.w2Part;
   const double za = pzA[k / Nb], ca = pcA[k / Nb], zb = pzB[k % Nb], cb = pcB[k % Nb];
-  const double Ck = ca * cb;
+  // derivative blocks: the product times zeta_a^max(0, shifta), then
+  // zeta_b^max(0, shiftb) (src/type2.c:456-462)
+  const double Ck = zeta_times(zeta_times(ca * cb, za, pa0), zb, pb0);
   double i1, i2;
   fm06(za, zb, dAC, dBC, i1, i2);
   const int nb = S.ppBreak[k], end = nb == INT_MAX ? OL - 1 : nb - 1;
@@ -649,7 +655,10 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   const int warp = tid >> 5;
   const int *wa = J.win + ((size_t)c * J.nShells + sa) * 3;
   const int *wb = J.win + ((size_t)c * J.nShells + sb) * 3;
-  if (wa[2] || wb[2]) {
+  // derivative shift: the shells' l moved by (shifta, shiftb) for the
+  // computation, the blocks handed out with l (lpa, lpb)
+  const UnitShift sh = unit_shift(J, pr, J.shL[sa], J.shL[sb], J.shAtom[sa], J.shAtom[sb], J.ctrAtom[c]);
+  if (wa[2] || wb[2] || sh.skip) {
     if (tid == 0) J.status[u] = kUnitSkipped;
     return;
   }
@@ -660,7 +669,8 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     return;
   }
   const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.nF, J.gcap);
-  const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa], lb = J.shL[sb], lab = la + lb;
+  const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa] + sh.a, lb = J.shL[sb] + sh.b, lab = la + lb;
+  const int lpa = sh.lpa, lpb = sh.lpb, pa0 = sh.a > 0 ? sh.a : 0, pb0 = sh.b > 0 ? sh.b : 0;
   const int nA = 2 * J.maxLBS + 1, LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE;
   const int Lc = J.ctrL[c], nca = NCUM(la), ncb = NCUM(lb), O = kSmallOrder;
   const size_t cA = (size_t)c * J.nAtoms + A, cB = (size_t)c * J.nAtoms + B;
@@ -671,7 +681,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   const int Na = J.shK[sa], Nb = J.shK[sb], NP = Na * Nb;
   double *chi = sm + Lm.chi, *Jsh = sm + Lm.J, *T = sm + Lm.T, *ph = sm + Lm.phase;
   double *out1 = J.out + (size_t)c * J.centreStride + J.pairOff[pr];
-  double *out2 = out1 + NCART(la) * NCART(lb);
+  double *out2 = out1 + NCART(lpa) * NCART(lpb);
   int warn1 = 0, warn2 = 0;
   if (tid == 0) S.warn = 0;
 
@@ -689,7 +699,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     }
     for (int p0 = warp * G; p0 < NP; p0 += kWarps * G)
       t1_group_run(J, Lm, W, c, Lc, la, lb, p0, NP - p0 < G ? NP - p0 : G, Nb, pzA, pcA, pzB, pcB, gA, gB,
-                   ws, we, warn1);
+                   ws, we, pa0, pb0, warn1);
     __syncthreads();
     // chi[i][j] = sum over warps of H[index(a_i + b_j)]
     const int dd = J.tmDim + 1;
@@ -703,11 +713,11 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     __syncthreads();
   }
   auto poly_shift = [&](double norm, double *dst) {  // src/util.c:247-334
-    const int D = J.uspD, dd = J.tmDim + 1, nta = NCART(la), ntb = NCART(lb);
+    const int D = J.uspD, dd = J.tmDim + 1, nta = NCART(lpa), ntb = NCART(lpb);
     const double *uA = J.usp + cA * D * D * D, *uB = J.usp + cB * D * D * D;
     for (int e = tid; e < nta * ncb; e += NT) {
       int c1 = e / ncb, q = e % ncb;
-      const int *ex = J.ijk + 3 * (NCUM(la - 1) + c1);
+      const int *ex = J.ijk + 3 * (NCUM(lpa - 1) + c1);
       double v = 0.0;
       for (int x = 0; x <= ex[0]; x++) {
         double bx = binom(J.fac, ex[0], x);
@@ -726,7 +736,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     __syncthreads();
     for (int e = tid; e < nta * ntb; e += NT) {
       int c1 = e / ntb, c2 = e % ntb;
-      const int *ex = J.ijk + 3 * (NCUM(lb - 1) + c2);
+      const int *ex = J.ijk + 3 * (NCUM(lpb - 1) + c2);
       double v = 0.0;
       for (int x = 0; x <= ex[0]; x++) {
         double bx = binom(J.fac, ex[0], x);
@@ -751,8 +761,10 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   // ---------------------------------------------------------- type 2
   const int nF = J.nF;
   double *Fa = ph + Lm.Fa, *Fb = ph + Lm.Fb;
-  const double *gFa = J.F + ((size_t)c * J.nShells + sa) * O * nF;
-  const double *gFb = J.F + ((size_t)c * J.nShells + sb) * O * nF;
+  // F tables of the derivative runs max(0, shift) (src/type2.c:563-564)
+  const int nRuns = J.nRuns > 0 ? J.nRuns : 1;
+  const double *gFa = J.F + (((size_t)c * J.nShells + sa) * nRuns + pa0) * O * nF;
+  const double *gFb = J.F + (((size_t)c * J.nShells + sb) * nRuns + pb0) * O * nF;
   for (int e = tid; e < O * nF; e += NT) { Fa[e] = gFa[e]; Fb[e] = gFb[e]; }
   for (int e = tid; e < LE * LBE * LBE * nA; e += NT) T[e] = 0.0;
   for (int e = tid; e < 64; e += NT) S.failMask[e] = 0;
@@ -829,7 +841,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       for (int q = tid & 31; q < nf; q += 32) W[Lm.w2Part + q] = 0.0;
       __syncwarp();
       for (int k = warp; k < NP; k += kWarps)
-        t2_pair(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, warn2);
+        t2_pair(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0, warn2);
       __syncthreads();
       for (int q = tid; q < nf; q += NT) {
         double v = 0.0;

@@ -87,7 +87,9 @@ __global__ void __launch_bounds__(64) k_centre_atom(DevJob J) {
   __shared__ double g[4];
   const int A = blockIdx.x, c = blockIdx.y;
   const int C = J.ctrAtom[c];
-  const int lA = J.atomMaxL[A], lmax = J.maxLECP - 1 + lA;
+  // the atom's largest l, plus the derivative order whose shifts raise it
+  // (src/libecp.c:285-286, :292-293)
+  const int lA = J.atomMaxL[A] + (J.deriv > 0 ? J.deriv : 0), lmax = J.maxLECP - 1 + lA;
   const size_t ca = (size_t)c * J.nAtoms + A;
   if (threadIdx.x == 0) {
     const double *rC = J.geom + 3 * C, *rA = J.geom + 3 * A;
@@ -149,23 +151,29 @@ __global__ void __launch_bounds__(128) k_shell_F(DevJob J) {
     w[0] = sw[0]; w[1] = sw[1]; w[2] = sw[2];
   }
   __syncthreads();
-  const int nF = J.nF, lmaxA = J.maxLECP - 1 + J.shL[s];
+  // run = derivative order of the table: rows up to L - 1 + l + run and
+  // coefficients times zeta^run (src/type2.c:229, :263-290)
+  const int nF = J.nF, nRuns = J.nRuns > 0 ? J.nRuns : 1;
   const double *pa = J.primA + J.shP[s], *pd = J.primD + J.shP[s];
-  double *F = J.F + ((size_t)c * J.nShells + s) * O * nF;
-  for (int n = threadIdx.x; n < O; n += blockDim.x) {
-    double acc[kMaxRows], K[kMaxRows];
-    for (int i = 0; i < nF; i++) acc[i] = 0.0;
-    if (!sw[2] && n >= sw[0] && n < sw[1] && lmaxA >= 0) {
-      double r = J.xSmall[n];
-      for (int p = 0; p < J.shK[s]; p++) {
-        double zeta = pa[p], da = pd[p];
-        bessel_eval(J, lmaxA, 2.0 * zeta * dAC * r, K, 1);
-        double e = dAC - r;
-        e = exp(-zeta * e * e);
-        for (int i = 0; i <= lmaxA; i++) acc[i] += da * K[i] * e;
+  for (int run = 0; run < nRuns; run++) {
+    const int lmaxA = J.maxLECP - 1 + J.shL[s] + run;
+    double *F = J.F + (((size_t)c * J.nShells + s) * nRuns + run) * O * nF;
+    for (int n = threadIdx.x; n < O; n += blockDim.x) {
+      double acc[kMaxRows], K[kMaxRows];
+      for (int i = 0; i < nF; i++) acc[i] = 0.0;
+      if (!sw[2] && n >= sw[0] && n < sw[1] && lmaxA >= 0) {
+        double r = J.xSmall[n];
+        for (int p = 0; p < J.shK[s]; p++) {
+          double zeta = pa[p], da = pd[p];
+          for (int k = 0; k < run; k++) da *= zeta;
+          bessel_eval(J, lmaxA, 2.0 * zeta * dAC * r, K, 1);
+          double e = dAC - r;
+          e = exp(-zeta * e * e);
+          for (int i = 0; i <= lmaxA; i++) acc[i] += da * K[i] * e;
+        }
       }
+      for (int i = 0; i < nF; i++) F[(size_t)n * nF + i] = acc[i];
     }
-    for (int i = 0; i < nF; i++) F[(size_t)n * nF + i] = acc[i];
   }
 }
 
@@ -189,7 +197,10 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
   const int sa = J.pairA[pr], sb = J.pairB[pr], tid = threadIdx.x, NT = blockDim.x;
   const int *wa = J.win + ((size_t)c * J.nShells + sa) * 3;
   const int *wb = J.win + ((size_t)c * J.nShells + sb) * 3;
-  if (wa[2] || wb[2]) {
+  // derivative shift: the shells' l moved by (shifta, shiftb) for the
+  // computation, the blocks handed out with l (lpa, lpb)
+  const UnitShift sh = unit_shift(J, pr, J.shL[sa], J.shL[sb], J.shAtom[sa], J.shAtom[sb], J.ctrAtom[c]);
+  if (wa[2] || wb[2] || sh.skip) {
     if (tid == 0) J.status[u] = kUnitSkipped;
     return;
   }
@@ -200,7 +211,8 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
     return;
   }
   const UnitSmem Lm = unit_smem_layout(J.maxLBS, J.maxLECP, J.nF);
-  const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa], lb = J.shL[sb];
+  const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa] + sh.a, lb = J.shL[sb] + sh.b;
+  const int lpa = sh.lpa, lpb = sh.lpb, pa0 = sh.a > 0 ? sh.a : 0, pb0 = sh.b > 0 ? sh.b : 0;
   const int lab = la + lb, nA = 2 * J.maxLBS + 1, LE = J.maxLECP > 0 ? J.maxLECP : 1;
   const int Lc = J.ctrL[c], nca = NCUM(la), ncb = NCUM(lb);
   const int Os = kSmallOrder, OL = J.largeOrder;
@@ -219,7 +231,7 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
   __shared__ int sDone[kMaxWalkers];
   W.done = sDone;
   double *out1 = J.out + (size_t)c * J.centreStride + J.pairOff[pr];
-  double *out2 = out1 + NCART(la) * NCART(lb);
+  double *out2 = out1 + NCART(lpa) * NCART(lpb);
   const double tol = J.tol;
   if (tid == 0) S.failed = 0;
 
@@ -227,7 +239,8 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
   for (int e = tid; e < nca * ncb; e += NT) chi[e] = 0.0;
   const int nq1 = [&] { int t = 0; for (int l1 = 0; l1 <= lab; l1++) t += l1 / 2 + 1; return t; }();
   for (int pp = 0; pp < Na * Nb; pp++) {
-    const double za = pzA[pp / Nb], ca = pcA[pp / Nb], zb = pzB[pp % Nb], cb = pcB[pp % Nb];
+    const double za = pzA[pp / Nb], zb = pzB[pp % Nb];
+    const double ca = zeta_times(pcA[pp / Nb], za, pa0), cb = zeta_times(pcB[pp % Nb], zb, pb0);
     if (tid == 0) {
       double P[3], Sp[3];
       for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * gA[i] + zb * gB[i]);
@@ -396,11 +409,11 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
 
   // binomial shift onto A and B (src/util.c:247-334); J then I
   auto poly_shift = [&](double norm, double *dst) {
-    const int D = J.uspD, dd = J.tmDim + 1, nta = NCART(la), ntb = NCART(lb);
+    const int D = J.uspD, dd = J.tmDim + 1, nta = NCART(lpa), ntb = NCART(lpb);
     const double *uA = J.usp + cA * D * D * D, *uB = J.usp + cB * D * D * D;
     for (int e = tid; e < nta * ncb; e += NT) {
       int c1 = e / ncb, q = e % ncb;
-      const int *ex = J.ijk + 3 * (NCUM(la - 1) + c1);
+      const int *ex = J.ijk + 3 * (NCUM(lpa - 1) + c1);
       double v = 0.0;
       for (int x = 0; x <= ex[0]; x++) {
         double bx = binom(J.fac, ex[0], x);
@@ -420,7 +433,7 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
     __syncthreads();
     for (int e = tid; e < nta * ntb; e += NT) {
       int c1 = e / ntb, c2 = e % ntb;
-      const int *ex = J.ijk + 3 * (NCUM(lb - 1) + c2);
+      const int *ex = J.ijk + 3 * (NCUM(lpb - 1) + c2);
       double v = 0.0;
       for (int x = 0; x <= ex[0]; x++) {
         double bx = binom(J.fac, ex[0], x);
@@ -446,8 +459,10 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
   // --------------------------------------------------------------- type 2
   const int nF = J.nF, LBE = J.maxLBS + LE;
   double *Fa = sm + Lm.Fa, *Fb = sm + Lm.Fb, *T = sm + Lm.T;
-  const double *gFa = J.F + ((size_t)c * J.nShells + sa) * Os * nF;
-  const double *gFb = J.F + ((size_t)c * J.nShells + sb) * Os * nF;
+  // F tables of the derivative runs max(0, shift) (src/type2.c:563-564)
+  const int nRuns = J.nRuns > 0 ? J.nRuns : 1;
+  const double *gFa = J.F + (((size_t)c * J.nShells + sa) * nRuns + pa0) * Os * nF;
+  const double *gFb = J.F + (((size_t)c * J.nShells + sb) * nRuns + pb0) * Os * nF;
   for (int e = tid; e < Os * nF; e += NT) { Fa[e] = gFa[e]; Fb[e] = gFb[e]; }
   for (int e = tid; e < LE * LBE * LBE * nA; e += NT) T[e] = 0.0;
   for (int e = tid; e < nca * ncb; e += NT) chi[e] = 0.0;
@@ -516,7 +531,7 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
       const int nf = S.anyFail, nextBase = S.nb;
       for (int k = 0; k < NP; k++) {
         const double za = pzA[k / Nb], ca = pcA[k / Nb], zb = pzB[k % Nb], cb = pcB[k % Nb];
-        const double Ck = ca * cb;
+        const double Ck = zeta_times(zeta_times(ca * cb, za, pa0), zb, pb0);
         const double zp = za + zb, Pm = (za * dAC + zb * dBC) / zp;
         const double sigma = 1.0 / sqrt(zp), t0 = Pm - 7.0 * sigma;
         const double rmin = (t0 > 0.0) ? t0 : 0.0, rmax = Pm + 9.0 * sigma;
@@ -735,7 +750,8 @@ void launch_prologue(const DevJob &J, cudaStream_t st) {
 }
 
 void launch_epilogue(const DevJob &J, cudaStream_t st) {
-  if (J.nPairs > 0) k_scatter<<<J.nPairs, 128, 0, st>>>(J);
+  // the AO matrix exists for derivative order 0 only (getIntegrals)
+  if (J.nPairs > 0 && J.deriv == 0) k_scatter<<<J.nPairs, 128, 0, st>>>(J);
 }
 
 }  // namespace ecpgb

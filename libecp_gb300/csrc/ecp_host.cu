@@ -50,6 +50,31 @@ void set_error(const char *fmt, ...) {
 
 // ------------------------------------------------------------------ parsing
 
+static const int kShiftA[3][10] = {{0}, {+1, -1, 0, 0}, {+2, -2, +1, +1, -1, -1, 0, 0, +1, 0}};
+static const int kShiftB[3][10] = {{0}, {0, 0, +1, -1}, {0, 0, +1, -1, +1, -1, +2, -2, 0, +1}};
+
+int shift_count(int deriv) { return deriv == 0 ? 1 : deriv == 1 ? 4 : 10; }
+
+void shift_pair(int deriv, int s, int &shifta, int &shiftb) {
+  shifta = kShiftA[deriv][s];
+  shiftb = kShiftB[deriv][s];
+}
+
+// The derivative scheme sizes every table for basis l up to maxLBS + n
+// (src/libecp.c:144-147): the tables of a job whose largest shell is shifted.
+TableKey table_key(const Parsed &P) {
+  return {P.maxLECP, P.maxLBS + P.deriv, P.largeGridOrder, P.tol, P.acc};
+}
+
+void shift_block_l(int deriv, int la, int lb, int shifta, int shiftb, int &lpa, int &lpb) {
+  lpa = la + shifta;
+  lpb = lb + shiftb;
+  if (deriv == 2) {
+    if (shifta == 1 && shiftb == 0) lpa = la;
+    else if (shifta == 0 && shiftb == 1) lpb = lb;
+  }
+}
+
 int parse_system(const ecpgb_system &s, Parsed &P) {
   P = Parsed();
   if (s.nrAtoms < 1 || !s.geometry || !s.shellsECP || !s.shellsBS) {
@@ -112,7 +137,19 @@ int parse_system(const ecpgb_system &s, Parsed &P) {
     P.maxLECP = std::max(P.maxLECP, L);
   }
   P.nCentres = (int)P.ctrAtom.size();
-  // shell pairs in the reference's loop order (src/libecp.c:278-312)
+  if (s.derivative < 0 || s.derivative > 2) {
+    set_error("derivative order %d outside 0..2", s.derivative);
+    return 1;
+  }
+  P.deriv = s.derivative;
+  P.nShift = shift_count(P.deriv);
+  if (P.maxLBS + P.deriv > kMaxLBasis) {  // the shifted shells must fit the tables
+    set_error("basis l %d with derivative order %d: shifted l above %d", P.maxLBS, P.deriv, kMaxLBasis);
+    return 1;
+  }
+  // shell pairs in the reference's loop order (src/libecp.c:278-312), each
+  // with its derivative shifts innermost (src/libecp.c:322); a shift that
+  // lowers l below 0 has no blocks
   long long off = 0;
   for (int A = 0; A < s.nrAtoms; A++)
     for (int B = A; B < s.nrAtoms; B++)
@@ -120,10 +157,17 @@ int parse_system(const ecpgb_system &s, Parsed &P) {
         for (int j = 0; j < s.shellsBS[B]; j++) {
           if (A == B && j < i) continue;
           int sa = P.atomShell0[A] + i, sb = P.atomShell0[B] + j;
-          P.pairA.push_back(sa);
-          P.pairB.push_back(sb);
-          P.pairOff.push_back(off);
-          off += 2LL * ncart(P.shL[sa]) * ncart(P.shL[sb]);
+          for (int k = 0; k < P.nShift; k++) {
+            int ha, hb, lpa, lpb;
+            shift_pair(P.deriv, k, ha, hb);
+            P.pairA.push_back(sa);
+            P.pairB.push_back(sb);
+            P.pairShift.push_back(k);
+            P.pairOff.push_back(off);
+            if (P.shL[sa] + ha < 0 || P.shL[sb] + hb < 0) continue;
+            shift_block_l(P.deriv, P.shL[sa], P.shL[sb], ha, hb, lpa, lpb);
+            off += 2LL * ncart(lpa) * ncart(lpb);
+          }
         }
   P.nPairs = (int)P.pairA.size();
   P.centreStride = off;
@@ -287,7 +331,7 @@ void schedules_overwritten() { engine().schedOwner = nullptr; }
 int engine_pin_request(const Parsed &P, const DevTables **T) {
   Engine &E = engine();
   if (E.ensure_init()) return 1;
-  const DevTables *t = E.get_tables({P.maxLECP, P.maxLBS, P.largeGridOrder, P.tol, P.acc});
+  const DevTables *t = E.get_tables(table_key(P));
   if (!t) return 1;
   if (E.schedPins > 0 && E.schedOwner != t && !(E.schedOwner && same_schedules(E.schedOwner, t))) return 4;
   if (E.use_schedules(t)) return 1;
@@ -350,13 +394,13 @@ static void unit_order(const Parsed &P, std::vector<int> &order) {
 // and fills the DevJob's input and work pointers.
 size_t job_device_bytes(const Parsed &P, int mode) {
   const size_t nc = P.nCentres, ns = P.nShells, na = P.nAtoms, O = kSmallOrder;
-  const size_t LE = P.maxLECP > 0 ? P.maxLECP : 1, LB = P.maxLBS;
+  const size_t LE = P.maxLECP > 0 ? P.maxLECP : 1, LB = P.maxLBS + P.deriv;
   const size_t nk = std::max(LB + LE, 2 * LB) + 1, nF = LB + LE + 1, D = LB + 1;  // table ranks (upper bounds)
   const size_t angLam = P.maxLECP + LB + 1, angC = (LB + 1) * (LB + 2) * (LB + 3) / 6;
   size_t in = 8 * (P.geom.size() + P.primA.size() + P.primD.size() + 3 * P.termL.size() + P.pairOff.size()) +
-              4 * (5 * P.shL.size() + P.atomMaxL.size() + 4 * P.ctrAtom.size() + P.termL.size() + 2 * P.pairA.size()) +
+              4 * (5 * P.shL.size() + P.atomMaxL.size() + 4 * P.ctrAtom.size() + P.termL.size() + 3 * P.pairA.size()) +
               (mode != ECPGB_FP64 ? 4 * nc * P.nPairs : 0) + 21 * 256;
-  size_t work = 8 * (ns + nc * O * LE * nk + nc * O + nc * ns * O * nF + nc * na * 4 + nc * na * D * D * D +
+  size_t work = 8 * (ns + nc * O * LE * nk + nc * O + nc * ns * (1 + P.deriv) * O * nF + nc * na * 4 + nc * na * D * D * D +
                      nc * na * angLam * LE * LE * angC + nc * (size_t)P.centreStride + (size_t)P.dim * P.dim) +
                 4 * (nc + nc * ns * 3 + nc * (size_t)P.nPairs + 2) + 8;
   return in + work;
@@ -396,7 +440,8 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
          iCA = add(P.ctrAtom.data(), 4 * P.ctrAtom.size()), iCL = add(P.ctrL.data(), 4 * P.ctrL.size()),
          iCT = add(P.ctrT0.data(), 4 * P.ctrT0.size()), iCN = add(P.ctrNT.data(), 4 * P.ctrNT.size()),
          iTL = add(P.termL.data(), 4 * P.termL.size()), iPrA = add(P.pairA.data(), 4 * P.pairA.size()),
-         iPrB = add(P.pairB.data(), 4 * P.pairB.size()), iPO = add(P.pairOff.data(), 8 * P.pairOff.size());
+         iPrB = add(P.pairB.data(), 4 * P.pairB.size()), iPO = add(P.pairOff.data(), 8 * P.pairOff.size()),
+         iPS = add(P.pairShift.data(), 4 * P.pairShift.size());
   std::vector<int> order;
   if (mode != ECPGB_FP64) unit_order(P, order);
   size_t iOrd = add(order.data(), 4 * order.size());
@@ -416,6 +461,9 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.ctrAtom = (const int *)dp(iCA); J.ctrL = (const int *)dp(iCL); J.ctrT0 = (const int *)dp(iCT);
   J.ctrNT = (const int *)dp(iCN); J.termL = (const int *)dp(iTL); J.pairA = (const int *)dp(iPrA);
   J.pairB = (const int *)dp(iPrB); J.pairOff = (const long long *)dp(iPO);
+  J.pairShift = (const int *)dp(iPS);
+  J.deriv = P.deriv;
+  J.nRuns = 1 + P.deriv;
   J.order = order.empty() ? nullptr : (const int *)dp(iOrd);
   J.centreStride = P.centreStride;
   // --- tables
@@ -426,7 +474,7 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   // --- work arrays
   const size_t nc = P.nCentres, ns = P.nShells, na = P.nAtoms, O = kSmallOrder;
   bool ok = B.radius.ensure(ns + 1) && B.utab.ensure(nc * O * LE * h.nk + 1) && B.uL.ensure(nc * O + 1) &&
-            B.gridEnd.ensure(nc + 1) && B.win.ensure(nc * ns * 3 + 1) && B.F.ensure(nc * ns * O * h.nF + 1) &&
+            B.gridEnd.ensure(nc + 1) && B.win.ensure(nc * ns * 3 + 1) && B.F.ensure(nc * ns * (1 + P.deriv) * O * h.nF + 1) &&
             B.cgeo.ensure(nc * na * 4 + 1) && B.usp.ensure(nc * na * J.uspD * J.uspD * J.uspD + 1) &&
             B.ang.ensure(nc * na * (size_t)J.angLam * J.angLM * J.angC + 1) &&
             B.out.ensure(nc * (size_t)P.centreStride + 1) && B.status.ensure(nc * (size_t)P.nPairs + 1) &&
@@ -482,11 +530,12 @@ int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_inf
   Parsed P;
   if (parse_system(s, P)) return 1;
   if (rowdim < P.dim) { set_error("rowdim %d < basis dimension %d", rowdim, P.dim); return 1; }
+  if (P.deriv) { set_error("the AO matrix exists for derivative order 0 only (use the blocks)"); return 1; }
   if (P.nCentres == 0 || P.nPairs == 0) {
     if (info) { std::memset(info, 0, sizeof *info); info->firstFailed = -1; }
     return 0;
   }
-  const DevTables *T = E.get_tables({P.maxLECP, P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
+  const DevTables *T = E.get_tables(table_key(P));
   if (!T || E.use_schedules(T, &lk)) return 1;
   JobBuffers &B = E.shared;
   DevJob J;
@@ -538,7 +587,7 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
     if (info) { std::memset(info, 0, sizeof *info); info->firstFailed = -1; }
     return 0;
   }
-  const DevTables *T = E.get_tables({P.maxLECP, P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
+  const DevTables *T = E.get_tables(table_key(P));
   if (!T || E.use_schedules(T, &lk)) return 1;
   JobBuffers &B = E.shared;
   DevJob J;
@@ -649,9 +698,10 @@ void *job_create(const ecpgb_system &s, int mode) {
   R->mode = mode;
   if (parse_system(s, R->P)) { delete R; return nullptr; }
   if (R->P.nCentres == 0 || R->P.nPairs == 0) { set_error("job has no units"); delete R; return nullptr; }
-  R->T = E.get_tables({R->P.maxLECP, R->P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy});
+  R->T = E.get_tables(table_key(R->P));
   if (!R->T || stage_job(R->P, R->T, R->B, R->J, mode, E.stream)) { delete R; return nullptr; }
   R->cfg = E.config_for(R->J.maxLBS, R->J.maxLECP);
+  R->launches = R->P.deriv ? 6 : 7;  // no AO scatter for derivative blocks
   // skipped units are never written: their values read as zero
   cudaMemsetAsync(R->B.out.p, 0, sizeof(double) * (size_t)R->P.nCentres * R->P.centreStride, E.stream);
   if (cudaStreamSynchronize(E.stream) != cudaSuccess) { set_error("staging failed"); delete R; return nullptr; }

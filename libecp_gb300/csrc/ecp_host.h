@@ -19,15 +19,29 @@ void set_error(const char *fmt, ...);
 struct Parsed {
   int nAtoms = 0, nShells = 0, nPrims = 0, nCentres = 0, nPairs = 0, dim = 0;
   int maxLECP = 0, maxLBS = 0, largeGridOrder = 1024;
+  // derivative order and its shifts: the pair list below holds every shell
+  // pair nShift times (pair-major, shift-minor, the reference's callback
+  // order), pairShift the shift index of each entry
+  int deriv = 0, nShift = 1;
   double tol = 1e-12, acc = 1e-14;
   std::vector<double> geom, primA, primD, termN, termD, termA;
   std::vector<int> shL, shK, shP, shAtom, shAO, shLocal, atomMaxL, atomShell0;
-  std::vector<int> ctrAtom, ctrL, ctrT0, ctrNT, termL, pairA, pairB;
+  std::vector<int> ctrAtom, ctrL, ctrT0, ctrNT, termL, pairA, pairB, pairShift;
   std::vector<long long> pairOff;
   long long centreStride = 0;
 };
 
 int parse_system(const ecpgb_system &s, Parsed &P);
+
+// Derivative shifts (src/libecp.c:240-248): number per order and the pair.
+int shift_count(int deriv);
+void shift_pair(int deriv, int s, int &shifta, int &shiftb);
+// Angular momenta of the blocks a shifted unit hands out: the shifted ones,
+// except the order-2 shifts (+1, 0) and (0, +1), whose blocks keep the
+// unshifted l (src/libecp.c:356-362).
+void shift_block_l(int deriv, int la, int lb, int shifta, int shiftb, int &lpa, int &lpb);
+struct TableKey;
+TableKey table_key(const Parsed &P);
 
 // Grow-only device buffer.
 template <class T>

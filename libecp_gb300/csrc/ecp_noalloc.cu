@@ -86,11 +86,12 @@ int run_matrix_noalloc(const ecpgb_system &s, int rowdim, double *I) {
   Parsed P;
   if (parse_system(s, P)) return 1;
   if (rowdim < P.dim) { set_error("rowdim %d < basis dimension %d", rowdim, P.dim); return 1; }
+  if (P.deriv) { set_error("the AO matrix exists for derivative order 0 only"); return 1; }
   if (P.nCentres == 0 || P.nPairs == 0) return 0;
   void *sp = nullptr;
   if (scratch_address(&sp)) return 1;
   HostTables h;
-  build_tables({P.maxLECP, P.maxLBS, s.largeGridOrder, s.tolerance, s.accuracy}, h);
+  build_tables(table_key(P), h);
   if (h.status) {
     set_error(h.status == 1 ? "Bessel series did not converge" : "table sizes out of range");
     return 1;

@@ -45,6 +45,8 @@ class EcpSystem:
     tolerance: float = 1.0e-12
     accuracy: float = 1.0e-14
     name: str = field(default="system")
+    # nuclear-derivative order of libECP_init (0, 1, 2): blocks of shifted shells
+    derivative: int = 0
 
     def __post_init__(self):
         self.geometry = np.ascontiguousarray(self.geometry, dtype=np.float64).reshape(-1)

@@ -151,6 +151,8 @@ def ref_lib(path=REF_SO):
                                                      ct.POINTER(ct.c_longlong)]
         lib.getIntegrals.argtypes = _sys_argtypes() + [ct.c_int, _D]
         lib.getIntegrals.restype = ct.c_int
+        lib.ref_blocks_deriv.argtypes = _sys_argtypes() + [ct.c_int, ct.c_int, _I, ct.c_longlong, _D, _I,
+                                                           ct.POINTER(ct.c_longlong)]
         _ref[path] = lib
     return _ref[path]
 
@@ -166,6 +168,21 @@ def ref_blocks(s, path=REF_SO):
     rc = lib.ref_blocks(*_sys_args(s), mb, meta.ctypes.data_as(_I), md, data.ctypes.data_as(_D),
                         ct.byref(nb), ct.byref(nd))
     return rc, meta[:8 * nb.value].reshape(-1, 8).copy(), data[:nd.value].copy()
+
+
+def ref_blocks_deriv(s, n, path=REF_SO):
+    """The reference's derivative blocks (libECP_init with derivative order n):
+    meta rows (A, s1, la, shifta, B, s2, lb, shiftb, C, type) and the data."""
+    lib = ref_lib(path)
+    mb, md = _capacity(s, None)
+    mb, md = 10 * mb, 80 * md  # up to 10 shifts, blocks of l + 2
+    meta = np.zeros(10 * mb, dtype=np.int32)
+    data = np.zeros(md, dtype=np.float64)
+    nb = ct.c_int(0)
+    nd = ct.c_longlong(0)
+    rc = lib.ref_blocks_deriv(*_sys_args(s), int(n), mb, meta.ctypes.data_as(_I), md,
+                              data.ctypes.data_as(_D), ct.byref(nb), ct.byref(nd))
+    return rc, meta[:10 * nb.value].reshape(-1, 10).copy(), data[:nd.value].copy()
 
 
 def ref_matrix(s, path=REF_SO):

@@ -79,3 +79,65 @@ int ref_blocks(int nrAtoms, double *geometry, int *shellsECP, int *KECP,
   if (r.overflow) return -2;
   return st;
 }
+
+/* ---- derivative blocks (libECP_init's n = 1, 2) ----
+ * The reference hands out, per (shell pair, centre) and derivative shift
+ * (shifta, shiftb), a type-1 and a type-2 block of the shifted shells
+ * (src/libecp.c:322-374); for n = 2 the shifts (+1, 0) and (0, +1) keep the
+ * unshifted l in the block (src/libecp.c:356-362).  Recorded with 10 ints per
+ * block: A, s1, la, shifta, B, s2, lb, shiftb, C, type. */
+typedef struct {
+  int n, maxBlocks, nBlocks;
+  int *meta;
+  long long maxData, nData;
+  double *data;
+  int overflow;
+  int lastKey[7];
+  int lastType;
+} DerivRecorder;
+
+static void record_deriv(int A, int sa, int la, int shifta, int B, int sb,
+                         int lb, int shiftb, int C, double *I, void *p) {
+  DerivRecorder *r = (DerivRecorder *)p;
+  int key[7] = {A, sa, B, sb, C, shifta, shiftb};
+  int type = 1, lpa = la + shifta, lpb = lb + shiftb;
+  if (r->n == 2 && shifta == 1 && shiftb == 0) lpa = la;
+  if (r->n == 2 && shifta == 0 && shiftb == 1) lpb = lb;
+  long long n = (long long)IJK(lpa) * IJK(lpb);
+  if (r->nBlocks > 0 && r->lastType == 1 && memcmp(key, r->lastKey, sizeof key) == 0)
+    type = 2;
+  memcpy(r->lastKey, key, sizeof key);
+  r->lastType = type;
+  if (r->nBlocks >= r->maxBlocks || r->nData + n > r->maxData) {
+    r->overflow = 1;
+    return;
+  }
+  int *m = r->meta + 10 * r->nBlocks;
+  m[0] = A; m[1] = sa; m[2] = la; m[3] = shifta; m[4] = B; m[5] = sb; m[6] = lb; m[7] = shiftb;
+  m[8] = C; m[9] = type;
+  memcpy(r->data + r->nData, I, n * sizeof(double));
+  r->nData += n;
+  r->nBlocks++;
+}
+
+int ref_blocks_deriv(int nrAtoms, double *geometry, int *shellsECP, int *KECP,
+                     int *lECP, double *nECP, double *dECP, double *aECP,
+                     int *shellsBS, int *lBS, int *KBS, double *dBS, double *aBS,
+                     int largeGridOrder, double tolerance, double accuracy, int n,
+                     int maxBlocks, int *meta, long long maxData, double *data,
+                     int *nBlocks, long long *nData) {
+  DerivRecorder r;
+  memset(&r, 0, sizeof r);
+  r.n = n; r.maxBlocks = maxBlocks; r.meta = meta; r.maxData = maxData; r.data = data;
+  libECPHandle *h = libECP_init(nrAtoms, geometry, shellsECP, lECP, KECP, nECP,
+                                dECP, aECP, shellsBS, lBS, KBS, dBS, aBS, n, -1,
+                                NULL, largeGridOrder, tolerance, accuracy);
+  if (h == NULL) return -1;
+  int st = calculateECPIntegrals(h, record_deriv, &r);
+  libECP_free(h);
+  *nBlocks = r.nBlocks;
+  *nData = r.nData;
+  if (r.overflow) return -2;
+  return st;
+}
+

@@ -13,6 +13,11 @@ reference with a zero-coefficient high-l pad centre (EcpSystem.padded), which
 keeps the reference's table reads in bounds and adds exactly zero; the blocks
 are those of the unpadded system.  The example-like fixture also stores the
 reference's getIntegrals matrix.
+
+The deriv*_ fixtures hold the nuclear-derivative blocks of libECP_init's
+order n (1 or 2): meta rows (A, s1, la, shifta, B, s2, lb, shiftb, C, type).
+Their systems keep basis l + n below the ECP's L, where the reference's
+tables stay in bounds without padding.
 """
 from __future__ import annotations
 
@@ -43,6 +48,28 @@ CASES = {
 }
 
 
+DERIV_CASES = {
+    "deriv1_s3": (1, lambda: W.random_system(3, n_atoms=3, n_centres=2, lmax_basis=2, lmax_ecp=4)),
+    "deriv1_s6": (1, lambda: W.random_system(6, n_atoms=4, n_centres=2, lmax_basis=1, lmax_ecp=3, kmax=3)),
+    "deriv2_s4": (2, lambda: W.random_system(4, n_atoms=3, n_centres=2, lmax_basis=1, lmax_ecp=4)),
+    "deriv2_s5": (2, lambda: W.random_system(5, n_atoms=3, n_centres=1, lmax_basis=2, lmax_ecp=5, kmax=2)),
+}
+
+
+def save_deriv(name, n, s):
+    assert s.max_l_basis() + n < s.max_l_ecp()
+    rc, meta, data = O.ref_blocks_deriv(s, n)
+    if rc != 0:
+        raise RuntimeError(f"reference failed on {name}: {rc}")
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"), geometry=s.geometry, shellsECP=s.shellsECP,
+        KECP=s.KECP, lECP=s.lECP, nECP=s.nECP, dECP=s.dECP, aECP=s.aECP, shellsBS=s.shellsBS,
+        lBS=s.lBS, KBS=s.KBS, dBS=s.dBS, aBS=s.aBS,
+        params=np.array([s.largeGridOrder, s.tolerance, s.accuracy]), derivative=np.array(n),
+        padded=np.array(False), meta=meta, data=data)
+    print(f"{name}: n={n}, {len(meta)} blocks, max|I|={np.abs(data).max():.3e}")
+
+
 def save(name, s):
     sr = s.padded() if s.needs_pad() else s
     rc, meta, data = O.ref_blocks(sr)
@@ -66,7 +93,8 @@ def load(path) -> tuple:
     p = z["params"]
     s = W.EcpSystem(z["geometry"], z["shellsECP"], z["KECP"], z["lECP"], z["nECP"], z["dECP"],
                     z["aECP"], z["shellsBS"], z["lBS"], z["KBS"], z["dBS"], z["aBS"],
-                    int(p[0]), float(p[1]), float(p[2]), name=os.path.basename(path))
+                    int(p[0]), float(p[1]), float(p[2]), name=os.path.basename(path),
+                    derivative=int(z["derivative"]) if "derivative" in z.files else 0)
     return s, z
 
 
@@ -74,6 +102,8 @@ if __name__ == "__main__":
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
     for name, make in CASES.items():
         save(name, make())
+    for name, (n, make) in DERIV_CASES.items():
+        save_deriv(name, n, make())
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         gcc = subprocess.run(["gcc", "--version"], capture_output=True, text=True).stdout.splitlines()[0]
         libc = " ".join(platform.libc_ver())

@@ -13,7 +13,13 @@ TOL_ABS = 1e-10
 
 
 def golden_files():
-    return sorted(f for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+    """Fixtures of derivative order 0."""
+    return sorted(f for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and not f.startswith("deriv"))
+
+
+def deriv_golden_files():
+    """Fixtures of the nuclear-derivative blocks (order 1 and 2)."""
+    return sorted(f for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and f.startswith("deriv"))
 
 
 def load_golden(name):
