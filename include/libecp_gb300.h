@@ -179,6 +179,22 @@ int ecpgb_server_get_stats(ecpgb_server *sv, ecpgb_server_stats *st);
 /* Finishes the jobs in flight and queued, then frees the server. */
 void ecpgb_server_free(ecpgb_server *sv);
 
+/* Readers for the text inputs of the reference's example program
+ * (example/ex1.c:12-123): an xyz file (count, comment, "symbol x y z" lines,
+ * coordinates used as given), an ECP file (per atom "index nCore nShells",
+ * per shell "l K", per term "index a d n" -- or "d a n", the three-number
+ * layout of the example's own ECP file, which the example's reader
+ * misparses) and a basis file (per atom "index nShells", per shell "l K", per
+ * primitive "index a d").  Every atom has an entry in both files.  The
+ * system gets largeGridOrder 1024, tolerance 1e-12, accuracy 1e-14 (the
+ * example's values, which the caller may change).  No GPU is needed.
+ * Returns NULL on a missing file or a malformed line (ecpgb_last_error). */
+typedef struct ecpgb_loaded ecpgb_loaded;
+ecpgb_loaded *ecpgb_load_system(const char *xyzPath, const char *ecpPath, const char *basisPath);
+const ecpgb_system *ecpgb_loaded_system(const ecpgb_loaded *L);
+const char *ecpgb_loaded_symbol(const ecpgb_loaded *L, int atom);
+void ecpgb_loaded_free(ecpgb_loaded *L);
+
 /* Pipe-throughput probe on the current device: out[0] FP64 FMA TFLOP/s,
  * out[1] FP32 FMA TFLOP/s, out[2] MUFU ex2 Gop/s, out[3] FP64 exp() Gop/s.
  * Takes about 0.5 s.  0 ok. */

@@ -135,6 +135,14 @@ def lib() -> ct.CDLL:
     L.ecpgb_server_get_stats.restype = ct.c_int
     L.ecpgb_server_free.argtypes = [ct.c_void_p]
     L.ecpgb_server_free.restype = None
+    L.ecpgb_load_system.argtypes = [ct.c_char_p, ct.c_char_p, ct.c_char_p]
+    L.ecpgb_load_system.restype = ct.c_void_p
+    L.ecpgb_loaded_system.argtypes = [ct.c_void_p]
+    L.ecpgb_loaded_system.restype = ct.POINTER(EcpgbSystem)
+    L.ecpgb_loaded_symbol.argtypes = [ct.c_void_p, ct.c_int]
+    L.ecpgb_loaded_symbol.restype = ct.c_char_p
+    L.ecpgb_loaded_free.argtypes = [ct.c_void_p]
+    L.ecpgb_loaded_free.restype = None
     L.ecpgb_job_free.restype = None
     L.ecpgb_measure_peaks.argtypes = [_D]
     L.ecpgb_last_error.restype = ct.c_char_p
@@ -478,3 +486,34 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def load_system(xyz: str, ecp: str, basis: str):
+    """Reads the example program's text inputs (ecpgb_load_system): returns
+    (EcpSystem, atom symbols).  No GPU needed."""
+    L = lib()
+    h = L.ecpgb_load_system(os.fsencode(xyz), os.fsencode(ecp), os.fsencode(basis))
+    if not h:
+        raise RuntimeError(f"ecpgb_load_system failed: {last_error()}")
+    try:
+        cs = L.ecpgb_loaded_system(h).contents
+        n = cs.nrAtoms
+        arr = lambda p, k, dt: np.ctypeslib.as_array(p, shape=(k,)).astype(dt).copy() if k else np.zeros(0, dt)
+        shellsECP = arr(cs.shellsECP, n, np.int32)
+        shellsBS = arr(cs.shellsBS, n, np.int32)
+        nse, nsb = int(shellsECP.sum()), int(shellsBS.sum())
+        KECP, lECP = arr(cs.KECP, nse, np.int32), arr(cs.lECP, nse, np.int32)
+        KBS, lBS = arr(cs.KBS, nsb, np.int32), arr(cs.lBS, nsb, np.int32)
+        nt, npr = int(KECP.sum()), int(KBS.sum())
+        from .workloads import EcpSystem as _Sys
+        s = _Sys(geometry=arr(cs.geometry, 3 * n, np.float64), shellsECP=shellsECP, KECP=KECP, lECP=lECP,
+                 nECP=arr(cs.nECP, nt, np.float64), dECP=arr(cs.dECP, nt, np.float64),
+                 aECP=arr(cs.aECP, nt, np.float64), shellsBS=shellsBS, lBS=lBS, KBS=KBS,
+                 dBS=arr(cs.dBS, npr, np.float64), aBS=arr(cs.aBS, npr, np.float64),
+                 largeGridOrder=cs.largeGridOrder, tolerance=cs.tolerance, accuracy=cs.accuracy,
+                 name=os.path.basename(xyz))
+        symbols = [L.ecpgb_loaded_symbol(h, i).decode() for i in range(n)]
+    finally:
+        L.ecpgb_loaded_free(h)
+    return s, symbols
+

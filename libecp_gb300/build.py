@@ -29,6 +29,7 @@ UNITS = [
     ("ecp_noalloc.cu", []),
     ("ecp_fast.cu", []),
     ("ecp_serve.cpp", []),
+    ("ecp_io.cpp", []),
 ]
 
 
