@@ -95,6 +95,16 @@ int ecpgb_blocks(const ecpgb_system *s, int mode, double *values, long long *off
 int ecpgb_getIntegrals(const ecpgb_system *s, int mode, int rowdim, double *I,
                        ecpgb_info *info);
 
+/* Device-side consumers of the blocks.  With a symmetric density matrix D
+ * (dim x dim, row stride ldD, the Cartesian AO order of getIntegrals):
+ * *energy = sum_{mu nu} D_{mu nu} V_{mu nu} of the ECP matrix V, and
+ * grad[3 * atom + k] = d energy / d R_{atom, k}, assembled on the GPU from the
+ * derivative-order-1 blocks (d/dA of a Cartesian Gaussian = 2 zeta g(a + 1_k)
+ * - a_k g(a - 1_k); the ECP centre by translational invariance), so only the
+ * 3 nAtoms numbers come back.  Either output may be NULL.  s->derivative is
+ * ignored.  0 ok, 1 error. */
+int ecpgb_gradient(const ecpgb_system *s, int mode, const double *D, int ldD, double *energy, double *grad);
+
 /* Device-resident job: inputs are copied to HBM once; ecpgb_job_run then
  * re-runs the whole pipeline (all kernels) nRuns times without host traffic,
  * writing one device-time per run (CUDA events on the engine's stream) to

@@ -135,6 +135,8 @@ def lib() -> ct.CDLL:
     L.ecpgb_server_get_stats.restype = ct.c_int
     L.ecpgb_server_free.argtypes = [ct.c_void_p]
     L.ecpgb_server_free.restype = None
+    L.ecpgb_gradient.argtypes = [P, ct.c_int, _D, ct.c_int, _D, _D]
+    L.ecpgb_gradient.restype = ct.c_int
     L.ecpgb_load_system.argtypes = [ct.c_char_p, ct.c_char_p, ct.c_char_p]
     L.ecpgb_load_system.restype = ct.c_void_p
     L.ecpgb_loaded_system.argtypes = [ct.c_void_p]
@@ -516,4 +518,18 @@ def load_system(xyz: str, ecp: str, basis: str):
     finally:
         L.ecpgb_loaded_free(h)
     return s, symbols
+
+
+def gradient(s: EcpSystem, D: np.ndarray, mode: int = ECPGB_FP64):
+    """(energy, gradient[nAtoms, 3]) of a symmetric density matrix D over the
+    ECP matrix, both contracted on the GPU (ecpgb_gradient)."""
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    assert D.shape == (s.dim, s.dim)
+    cs = c_system(s)
+    e = ct.c_double(0.0)
+    g = np.zeros((s.n_atoms, 3))
+    if lib().ecpgb_gradient(ct.byref(cs), mode, D.ctypes.data_as(_D), s.dim, ct.byref(e),
+                            g.ctypes.data_as(_D)):
+        raise RuntimeError(f"ecpgb_gradient failed: {last_error()}")
+    return e.value, g
 

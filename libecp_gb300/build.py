@@ -30,6 +30,7 @@ UNITS = [
     ("ecp_fast.cu", []),
     ("ecp_serve.cpp", []),
     ("ecp_io.cpp", []),
+    ("ecp_grad.cu", []),
 ]
 
 

@@ -188,6 +188,11 @@ int ecpgb_blocks(const ecpgb_system *s, int mode, double *values, long long *off
   return ecpgb::run_blocks(*s, mode, values, offsets, status, info, nullptr) ? 1 : 0;
 }
 
+int ecpgb_gradient(const ecpgb_system *s, int mode, const double *D, int ldD, double *energy, double *grad) {
+  if (!s || !D) { ecpgb::set_error("null system or density matrix"); return 1; }
+  return ecpgb::run_gradient(*s, mode, D, ldD, energy, grad);
+}
+
 int ecpgb_getIntegrals(const ecpgb_system *s, int mode, int rowdim, double *I, ecpgb_info *info) {
   if (!s) return 1;
   int rc = ecpgb::run_matrix(*s, mode, rowdim, I, info);

@@ -155,6 +155,12 @@ inline void record_timing(cudaEvent_t e, cudaStream_t st) {
   else cudaEventRecord(e, st);
 }
 
+// Device-side consumers (ecp_grad.cu): the gradient contraction of an
+// order-1 job's blocks with a density matrix (added to grad[3 * nAtoms]), and
+// the energy of the upper-triangle AO matrix V.
+void launch_gradient(const DevJob &J, const double *D, int ldD, double *grad, cudaStream_t st);
+void launch_energy(const double *V, int dim, const double *D, int ldD, double *E, cudaStream_t st);
+
 // Launchers return 0, 3 when the shared memory does not fit, or
 // kLaunchErrorBase + the cudaError_t of a failed launch.
 constexpr int kLaunchErrorBase = 1000;

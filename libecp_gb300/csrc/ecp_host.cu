@@ -215,6 +215,7 @@ struct Engine {
   const DevTables *schedOwner = nullptr;
   JobBuffers shared;
   DBuf<char> flush;
+  DBuf<double> dens, gradBuf;  // density matrix and gradient of run_gradient
   bool init = false;
 
   int ensure_init() {
@@ -627,6 +628,54 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
     info->d2hBytes = (long long)(sizeof(double) * nv + sizeof(int) * nUnits);
   }
   if (err1) { set_error("a shell radius did not converge (Newton, 40 steps)"); return 1; }
+  return 0;
+}
+
+// Energy and nuclear gradient of a density matrix (device-side consumers,
+// ecp_grad.cu): the order-0 pipeline for E, the order-1 pipeline for the
+// gradient, each contracted with D on the GPU.
+int run_gradient(const ecpgb_system &s0, int mode, const double *D, int ldD, double *energy, double *grad) {
+  Engine &E = engine();
+  std::unique_lock<std::mutex> lk(E.mu);
+  if (!valid_mode(mode)) { set_error("unknown mode %d", mode); return 1; }
+  if (E.ensure_init()) return 1;
+  ecpgb_system s = s0;
+  for (int order : {0, 1}) {
+    if (order == 0 && !energy) continue;
+    if (order == 1 && !grad) continue;
+    s.derivative = order;
+    Parsed P;
+    if (parse_system(s, P)) return 1;
+    if (ldD < P.dim) { set_error("ldD %d < basis dimension %d", ldD, P.dim); return 1; }
+    const size_t nD = (size_t)P.dim * ldD;
+    if (!E.dens.ensure(nD + 1) || !E.gradBuf.ensure(3 * (size_t)P.nAtoms + 1)) {
+      set_error("device allocation failed");
+      return 1;
+    }
+    if (P.nCentres == 0 || P.nPairs == 0) {
+      if (order == 0) *energy = 0.0;
+      else std::memset(grad, 0, sizeof(double) * 3 * P.nAtoms);
+      continue;
+    }
+    const DevTables *T = E.get_tables(table_key(P));
+    if (!T || E.use_schedules(T, &lk)) return 1;
+    JobBuffers &B = E.shared;
+    DevJob J;
+    if (stage_job(P, T, B, J, mode, E.stream)) return 1;
+    CUDA_OK(cudaMemcpyAsync(E.dens.p, D, sizeof(double) * nD, cudaMemcpyHostToDevice, E.stream));
+    if (run_pipeline(B, J, mode, nullptr, nullptr, nullptr, E.stream)) return 1;
+    if (order == 0) {
+      launch_energy(B.mat.p, P.dim, E.dens.p, ldD, E.gradBuf.p, E.stream);
+      CUDA_OK(cudaMemcpyAsync(energy, E.gradBuf.p, sizeof(double), cudaMemcpyDeviceToHost, E.stream));
+    } else {
+      CUDA_OK(cudaMemsetAsync(E.gradBuf.p, 0, sizeof(double) * 3 * P.nAtoms, E.stream));
+      launch_gradient(J, E.dens.p, ldD, E.gradBuf.p, E.stream);
+      CUDA_OK(cudaMemcpyAsync(grad, E.gradBuf.p, sizeof(double) * 3 * P.nAtoms, cudaMemcpyDeviceToHost,
+                              E.stream));
+    }
+    cudaError_t ce = cudaStreamSynchronize(E.stream);
+    if (ce != cudaSuccess) { set_error("device error: %s", cudaGetErrorString(ce)); return 1; }
+  }
   return 0;
 }
 

@@ -117,6 +117,7 @@ int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_inf
 int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offsets, int *status,
                ecpgb_info *info, Parsed *parsedOut);
 int layout(const ecpgb_system &s, long long *nUnits, long long *nValues);
+int run_gradient(const ecpgb_system &s, int mode, const double *D, int ldD, double *energy, double *grad);
 void *job_create(const ecpgb_system &s, int mode);
 int job_run(void *j, int nRuns, int flushL2, float *msRun, float *msUnit);
 int job_matrix(void *j, int rowdim, double *I);
