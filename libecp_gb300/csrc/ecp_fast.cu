@@ -17,6 +17,8 @@
 //     depends on (i, j) only through the index of a_i + b_j
 //     (src/type1.c:323-345), so one accumulator per combined index receives
 //     exactly the terms the reference adds to each chi[i][j].
+#include <algorithm>
+
 #include "ecp_device.cuh"
 #include "ecp_fastmath.h"
 
@@ -24,6 +26,11 @@ namespace ecpgb {
 
 constexpr int kWarps = kUnitThreads / 32;
 constexpr int kWalkCap = 128;  // large-grid quadratures per warp and pass
+
+// The small-grid schedule's slots step by step (33, then 32 at a time) in
+// ascending order of their grid point: a unit's window [ws, we) is then one
+// run of each step, so its points can be dealt to consecutive lanes.
+static __constant__ short c93_byN[kSmallOrder];
 // Mixed mode: FP32 integrands carry noise of a few 1e-8 relative, below which
 // no error estimate can fall, so a quadrature also stops once its estimated
 // error is below kMixedRel of its value -- from kMixedMinPoints points on
@@ -384,24 +391,36 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
   int k = 0, cnt = 0;
   for (int s0 = 0; s0 < O;) {
     const int s1 = step_end93(s0) < O ? step_end93(s0) : O;
-    for (int e = lane; e < (s1 - s0) * G; e += 32) {
-      const int t = s0 + e / G, gg = e % G, n = c93_slot[t];
-      double *ent = tab + e * TSs;
-      // slot entry: [0, lq) K_l(s r), [lq, 2lq) w * C1 U_L e^(..) r^l
-      if (n >= ws && n < we) {
-        const double s = sc[gg * 6];
-        double r = J.xSmall[n], ex = (sc[gg * 6 + 4] * r + s) * r;
-        ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
-        const double wB = J.wSmall[n] * (sc[gg * 6 + 3] * uL[n] * ex);
-        bessel_fast(J, lab, s * r, ent, 1);
-        double *WR = ent + lq, rl = 1.0;
-        for (int l = 0; l <= lab; l++) {
-          WR[l] = wB * rl;
-          rl = r * rl;
-        }
-      } else {
-        for (int l = 0; l < 2 * lq; l++) ent[l] = 0.0;
+    // slot entry: [0, lq) K_l(s r), [lq, 2lq) w * C1 U_L e^(..) r^l; zero
+    // outside the window.  The step's in-window slots are the run [lo, hi)
+    // of its by-point order, dealt to consecutive lanes.
+    const int ns = s1 - s0;
+    int lo, hi;
+    {
+      const int n0 = lane < ns ? c93_slot[c93_byN[s0 + lane]] : INT_MAX;
+      const int n1 = lane + 32 < ns ? c93_slot[c93_byN[s0 + lane + 32]] : INT_MAX;
+      lo = __popc(__ballot_sync(0xffffffffu, n0 < ws)) + __popc(__ballot_sync(0xffffffffu, n1 < ws));
+      hi = __popc(__ballot_sync(0xffffffffu, n0 < we)) + __popc(__ballot_sync(0xffffffffu, n1 < we));
+    }
+    const int nIn = hi - lo;
+    for (int e = lane; e < nIn * G; e += 32) {
+      const int gg = e % G, t = c93_byN[s0 + lo + e / G], n = c93_slot[t];
+      double *ent = tab + ((t - s0) * G + gg) * TSs;
+      const double s = sc[gg * 6];
+      double r = J.xSmall[n], ex = (sc[gg * 6 + 4] * r + s) * r;
+      ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
+      const double wB = J.wSmall[n] * (sc[gg * 6 + 3] * uL[n] * ex);
+      bessel_fast(J, lab, s * r, ent, 1);
+      double *WR = ent + lq, rl = 1.0;
+      for (int l = 0; l <= lab; l++) {
+        WR[l] = wB * rl;
+        rl = r * rl;
       }
+    }
+    for (int e = lane; e < (ns - nIn) * G; e += 32) {
+      const int i = e / G, t = c93_byN[s0 + (i < lo ? i : i + nIn)];
+      double *ent = tab + ((t - s0) * G + e % G) * TSs;
+      for (int l = 0; l < 2 * lq; l++) ent[l] = 0.0;
     }
     __syncwarp();
     auto ent_of = [&](int t) { return tab + ((t - s0) * G + g) * TSs; };
@@ -932,6 +951,16 @@ int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, con
                           const int *s92lvEnd, const int *s92lvN, int s92levels, void *stream) {
   if (s93n > kSmallOrder || s92n > kMaxLargeOrder || s93levels > 32 || s92levels > 32) return 1;
   cudaStream_t st = (cudaStream_t)stream;
+  // each step's slots by ascending grid point (the steps of t1_group_run)
+  static short byN[kSmallOrder];
+  for (int s0 = 0; s0 < s93n;) {
+    int s1 = s0 == 0 ? 33 : s0 + 32;
+    if (s1 > s93n) s1 = s93n;
+    for (int t = s0; t < s1; t++) byN[t] = (short)t;
+    std::sort(byN + s0, byN + s1, [&](short a, short b) { return s93slot[a] < s93slot[b]; });
+    s0 = s1;
+  }
+  cudaMemcpyToSymbolAsync(c93_byN, byN, sizeof(short) * s93n, 0, cudaMemcpyHostToDevice, st);
   cudaMemcpyToSymbolAsync(c93_slot, s93slot, sizeof(int) * s93n, 0, cudaMemcpyHostToDevice, st);
   cudaMemcpyToSymbolAsync(c93_lvEnd, s93lvEnd, sizeof(int) * s93levels, 0, cudaMemcpyHostToDevice, st);
   cudaMemcpyToSymbolAsync(c93_lvJ, s93lvJ, sizeof(int) * s93levels, 0, cudaMemcpyHostToDevice, st);
