@@ -26,6 +26,8 @@ namespace ecpgb {
 
 constexpr int kWarps = kUnitThreads / 32;
 constexpr int kWalkCap = 128;  // large-grid quadratures per warp and pass
+constexpr int kLargeWords = (kMaxLargeOrder + 1) / 32;  // bitmap words over the large grid (128, even)
+static_assert(kLargeWords * 32 >= kMaxLargeOrder && kLargeWords % 2 == 0, "large-grid bitmap size");
 
 // The small-grid schedule's slots step by step (33, then 32 at a time) in
 // ascending order of their grid point: a unit's window [ws, we) is then one
@@ -234,6 +236,7 @@ struct FastSmem {
   int Fa, Fb;
   // type-2 fallback per warp (inside phase)
   int w2Stride, w2Tab, w2I, w2P, w2Q, w2R, w2Part, tab2Stride;
+  int w2Bits, w2Pend, w2Pref;  // fallback streaming: needed-slot bitmap, pending slots, word prefixes
 };
 
 __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap) {
@@ -273,7 +276,10 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap)
   s.w2Q = s.w2P + kWalkCap;
   s.w2R = s.w2Q + kWalkCap;
   s.w2Part = s.w2R + kWalkCap;
-  s.w2Stride = s.w2Part + kWalkCap;
+  s.w2Bits = s.w2Part + kWalkCap;            // kLargeWords uint32
+  s.w2Pend = s.w2Bits + kLargeWords / 2;      // 64 int
+  s.w2Pref = s.w2Pend + 32;                   // kLargeWords int
+  s.w2Stride = s.w2Pref + kLargeWords / 2;
   int t2b = kWarps * s.w2Stride;
   int ph = t1;
   if (t2a > ph) ph = t2a;
@@ -583,6 +589,8 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
   const int TS = L.tab2Stride;
   double *tab = W + L.w2Tab, *sI = W + L.w2I, *sP = W + L.w2P, *sQ = W + L.w2Q, *sR = W + L.w2R;
   double *part = W + L.w2Part;
+  unsigned *needBits = (unsigned *)(W + L.w2Bits);
+  int *pend = (int *)(W + L.w2Pend), *pref = (int *)(W + L.w2Pref);
   const double za = pzA[k / Nb], ca = pcA[k / Nb], zb = pzB[k % Nb], cb = pcB[k % Nb];
   // derivative blocks: the product times zeta_a^max(0, shifta), then
   // zeta_b^max(0, shiftb) (src/type2.c:456-462)
@@ -591,43 +599,88 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
   fm06(za, zb, dAC, dBC, i1, i2);
   const int nb = S.ppBreak[k], end = nb == INT_MAX ? OL - 1 : nb - 1;
   for (int q = lane; q < nf; q += 32) { sI[q] = 0; sP[q] = 0; sQ[q] = 0; sR[q] = 0; }
+  for (int w = lane; w < (OL + 31) / 32; w += 32) needBits[w] = 0u;
   __syncwarp();
+  // Whose tables slot t reads (the reference's reused buffers): this pair's
+  // below its break; beyond it, on the lower half, the last earlier pair
+  // whose loop reached that point; and the point, exponent of that pair.
+  auto locate = [&](int t, int &owner, double &r, double &ex) {
+    const int n = c92_slot[t];
+    const bool upper = t > 0 && ((t - 1) & 1);
+    owner = -1;
+    if (n < nb) owner = k;
+    else if (n != nb && !upper) {
+      for (int j = k - 1; j >= 0; j--)
+        if (S.ppBreak[j] >= n) { owner = j; break; }
+      if (owner >= 0 && S.ppBreak[owner] == n) owner = -1;
+    }
+    if (owner < 0) return;
+    const double zaj = pzA[owner / Nb], zbj = pzB[owner % Nb];
+    double i1j = i1, i2j = i2;
+    if (owner != k) fm06(zaj, zbj, dAC, dBC, i1j, i2j);
+    r = i1j * J.xLarge[n] + i2j;
+    const double d1 = dAC - r, d2 = dBC - r;
+    ex = -zaj * d1 * d1 - zbj * d2 * d2;
+  };
+  // A slot needs its tables only where they are not negligible; the others
+  // integrate to exactly zero.  Slots are classified step by step (cheap),
+  // the needed ones queued, and each pass evaluates 32 queued slots, one per
+  // lane, before the quadratures walk every slot up to the first one still
+  // queued.
   unsigned doneBits[kWalkCap / 32] = {0u, 0u, 0u, 0u};
-  for (int s0 = 0; s0 < OL;) {
-    const int s1 = step_end92(s0) < OL ? step_end92(s0) : OL;
-    for (int t = s0 + lane; t < s1; t += 32) {
-      int n = c92_slot[t];
-      bool upper = t > 0 && ((t - 1) & 1);
-      double *e = tab + (t - s0) * TS;
-      double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
-      e[0] = J.wLarge[n] * i1;
-      e[1] = 0.0;
-      e[2] = (!upper || n <= end) ? 1.0 : 0.0;
-      int owner = -1;
-      if (n < nb) owner = k;
-      else if (n != nb && !upper) {
-        for (int j = k - 1; j >= 0; j--)
-          if (S.ppBreak[j] >= n) { owner = j; break; }
-        if (owner >= 0 && S.ppBreak[owner] == n) owner = -1;
+  int cpos = 0, wpos = 0, nPend = 0;
+  const unsigned below = (1u << lane) - 1u;
+  while (wpos < OL) {
+    while (nPend < 32 && cpos < OL) {
+      const int c1 = step_end92(cpos) < OL ? step_end92(cpos) : OL, t = cpos + lane;
+      bool need = false;
+      if (t < c1) {
+        int owner;
+        double r, ex;
+        locate(t, owner, r, ex);
+        need = owner >= 0 && ex >= J.lnAcc2;
       }
-      if (owner >= 0) {
-        const double zaj = pzA[owner / Nb], zbj = pzB[owner % Nb];
-        double i1j = i1, i2j = i2;
-        if (owner != k) fm06(zaj, zbj, dAC, dBC, i1j, i2j);
-        double r = i1j * J.xLarge[n] + i2j, d1 = dAC - r, d2 = dBC - r;
-        double ex = -zaj * d1 * d1 - zbj * d2 * d2;
-        if (ex >= J.lnAcc2) {
-          // Ka rows carry the weight and prefactor: w * Ck * e^(..) * K_l1
-          const double wB = e[0] * (Ck * fast_exp(ex));
-          e[1] = 1.0;
-          // only the channels and rows this pass's quadratures read
-          channels_masked(J, c, r, S.passMask, U);
-          bessel_fast(J, S.passL1, 2.0 * zaj * dAC * r, Ka, 1);
-          for (int l = 0; l <= S.passL1; l++) Ka[l] *= wB;
-          bessel_fast(J, S.passL2, 2.0 * zbj * dBC * r, Kb, 1);
-          R[0] = 1.0;
-          for (int l = 1; l <= S.passL3; l++) R[l] = r * R[l - 1];
-        }
+      const unsigned m = __ballot_sync(0xffffffffu, need);
+      if (need) {
+        pend[nPend + __popc(m & below)] = t;
+        atomicOr(&needBits[t >> 5], 1u << (t & 31));
+      }
+      nPend += __popc(m);
+      cpos = c1;
+    }
+    __syncwarp();
+    // this pass: the first queued slots, and the walk's end: an odd slot
+    // (whole (lower, upper) pairs) that no queued slot precedes
+    int nE = nPend < 32 ? nPend : 32, b = cpos;
+    if (nPend > 32) {
+      b = pend[32];
+      if (!(b & 1)) b -= 1;
+      while (nE > 0 && pend[nE - 1] >= b) nE--;
+    }
+    if (lane < nE) {
+      const int t = pend[lane], n = c92_slot[t];
+      int owner;
+      double r, ex;
+      locate(t, owner, r, ex);
+      const double zaj = pzA[owner / Nb], zbj = pzB[owner % Nb];
+      double *e = tab + lane * TS;
+      double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
+      // Ka rows carry the weight and prefactor: w * Ck * e^(..) * K_l1
+      const double wB = (J.wLarge[n] * i1) * (Ck * fast_exp(ex));
+      // only the channels and rows this pass's quadratures read
+      channels_masked(J, c, r, S.passMask, U);
+      bessel_fast(J, S.passL1, 2.0 * zaj * dAC * r, Ka, 1);
+      for (int l = 0; l <= S.passL1; l++) Ka[l] *= wB;
+      bessel_fast(J, S.passL2, 2.0 * zbj * dBC * r, Kb, 1);
+      R[0] = 1.0;
+      for (int l = 1; l <= S.passL3; l++) R[l] = r * R[l - 1];
+    }
+    if (lane == 0) {  // entry of slot t: queued slots in [wpos, t)
+      const int w0 = wpos >> 5, w1 = (b - 1) >> 5;
+      int acc = -__popc(needBits[w0] & ((1u << (wpos & 31)) - 1u));
+      for (int w = w0; w <= w1; w++) {
+        pref[w] = acc;
+        acc += __popc(needBits[w]);
       }
     }
     __syncwarp();
@@ -639,21 +692,29 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       int it = J.items[J.itemOff[ncls + l] + qq];
       int l1 = it & 255, l2 = (it >> 8) & 255, l3 = it >> 16;
       auto val = [&](int t) {
-        const double *e = tab + (t - s0) * TS;
-        if (e[1] == 0.0) return 0.0;
+        const unsigned word = needBits[t >> 5], bit = 1u << (t & 31);
+        if (!(word & bit)) return 0.0;
+        const double *e = tab + (pref[t >> 5] + __popc(word & (bit - 1u))) * TS;
         const double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
         return Ka[l1] * Kb[l2] * U[l] * R[l3];
       };
-      auto vis = [&](int t) { return tab[(t - s0) * TS + 2] != 0.0; };
+      auto vis = [&](int t) { return !(t > 0 && ((t - 1) & 1)) || c92_slot[t] <= end; };
       double I = sI[q], p = sP[q], qv = sQ[q], res = 0;
       bool done = false;
-      psm92_advance(s0, s1, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
+      psm92_advance(wpos, b, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
       sI[q] = I; sP[q] = p; sQ[q] = qv;
       if (done) { sR[q] = res; doneBits[qi] |= 1u << lane; }
       else all = false;
     }
+    // drop the evaluated slots from the queue
+    const int rest = nPend - nE;
+    const int keep0 = lane < rest ? pend[nE + lane] : 0, keep1 = lane + 32 < rest ? pend[nE + lane + 32] : 0;
     __syncwarp();
-    s0 = s1;
+    if (lane < rest) pend[lane] = keep0;
+    if (lane + 32 < rest) pend[lane + 32] = keep1;
+    nPend = rest;
+    wpos = b;
+    __syncwarp();
     if (__all_sync(0xffffffffu, all)) break;
   }
   const double Nlast = c92_lvN[c92_nLevels - 1] + 1.0;
