@@ -38,6 +38,13 @@ typedef struct {
    * Cartesian shells with coefficients times zeta^max(0, shift).  The AO
    * matrix (getIntegrals, ecpgb_getIntegrals) exists for n = 0 only. */
   int derivative;
+  /* libECP_init's Cartesian order (src/libecp.h:15-21): NULL for libint's,
+   * else the exponent triples of every Cartesian function of shells
+   * l = 0..orderingLmax, shell by shell, in the caller's order within each
+   * shell; blocks and the matrix then come out in that order.  The reference
+   * requires orderingLmax >= maxL_ECP + 2 (max basis l + n) (src/libecp.c:159). */
+  const int *shellOrdering;
+  int orderingLmax;
 } ecpgb_system;
 
 enum {

@@ -33,7 +33,8 @@ class EcpgbSystem(ct.Structure):
     _fields_ = [("nrAtoms", ct.c_int), ("geometry", _D), ("shellsECP", _I), ("KECP", _I),
                 ("lECP", _I), ("nECP", _D), ("dECP", _D), ("aECP", _D), ("shellsBS", _I),
                 ("lBS", _I), ("KBS", _I), ("dBS", _D), ("aBS", _D), ("largeGridOrder", ct.c_int),
-                ("tolerance", ct.c_double), ("accuracy", ct.c_double), ("derivative", ct.c_int)]
+                ("tolerance", ct.c_double), ("accuracy", ct.c_double), ("derivative", ct.c_int),
+                ("shellOrdering", _I), ("orderingLmax", ct.c_int)]
 
 
 class EcpgbInfo(ct.Structure):
@@ -167,8 +168,14 @@ def _ptrs(s: EcpSystem):
 
 def c_system(s: EcpSystem) -> EcpgbSystem:
     p = _ptrs(s)
+    order = getattr(s, "ordering", None)
+    if order is not None:
+        order = np.ascontiguousarray(order, dtype=np.int32)
+        s._ordering_c = order  # keep the buffer alive with the system
     return EcpgbSystem(p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9], p[10], p[11],
-                       p[12], p[13], p[14], p[15], int(getattr(s, "derivative", 0)))
+                       p[12], p[13], p[14], p[15], int(getattr(s, "derivative", 0)),
+                       order.ctypes.data_as(_I) if order is not None else None,
+                       int(getattr(s, "ordering_lmax", 0)) if order is not None else 0)
 
 
 def get_integrals(s: EcpSystem, I: np.ndarray | None = None) -> np.ndarray:
@@ -307,9 +314,14 @@ def calculate_blocks_via_callback(s: EcpSystem):
     L = lib()
     p = _ptrs(s)
     n = int(getattr(s, "derivative", 0))
+    order = getattr(s, "ordering", None)
+    lmax, optr = -1, None
+    if order is not None:
+        order = np.ascontiguousarray(order, dtype=np.int32)
+        lmax, optr = int(s.ordering_lmax), order.ctypes.data_as(_I)
     # libECP_init reads (shellsECP, lECP, KECP) -- the definition's order
     h = L.libECP_init(p[0], p[1], p[2], p[4], p[3], p[5], p[6], p[7], p[8], p[9], p[10], p[11],
-                      p[12], n, -1, None, p[13], p[14], p[15])
+                      p[12], n, lmax, optr, p[13], p[14], p[15])
     if not h:
         raise RuntimeError(f"libECP_init failed: {last_error()}")
     meta, data = [], []
@@ -488,6 +500,17 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def libint_ordering(lmax: int) -> np.ndarray:
+    """libint's Cartesian order of shells 0..lmax as exponent triples (the
+    default order; a shellOrdering is a permutation within each shell)."""
+    out = []
+    for l in range(lmax + 1):
+        for i in range(l + 1):
+            for j in range(i + 1):
+                out += [l - i, i - j, j]
+    return np.array(out, dtype=np.int32)
 
 
 def load_system(xyz: str, ecp: str, basis: str):

@@ -28,6 +28,7 @@ struct _libECPHandle {
   ecpgb_system sys;
   std::vector<int> shellsECP, KECP, lECP;  // ECP arrays are copied, as the reference copies its ECPs
   std::vector<double> nECP, dECP, aECP;
+  std::vector<int> ordering;               // copied too (the reference keeps the caller's pointer)
 };
 
 struct ecpgb_job {
@@ -55,13 +56,8 @@ libECPHandle *libECP_init(int nrAtoms, double *geometry, int *shellsECP, int *lE
                           double *nECP, double *dECP, double *aECP, int *shellsBS, int *lBS,
                           int *KBS, double *dBS, double *aBS, int n, int lmax, int *shellOrdering,
                           int largeGridOrder, double tolerance, double accuracy) {
-  (void)lmax;
   if (n < 0 || n > 2) {  // the reference's shift table covers orders 0..2 (src/libecp.c:243-248)
     ecpgb::set_error("derivative order %d outside 0..2", n);
-    return nullptr;
-  }
-  if (shellOrdering != nullptr) {
-    ecpgb::set_error("custom Cartesian orderings are not implemented (pass NULL)");
     return nullptr;
   }
   if (nrAtoms < 1) return nullptr;
@@ -77,7 +73,17 @@ libECPHandle *libECP_init(int nrAtoms, double *geometry, int *shellsECP, int *lE
   h->aECP.assign(aECP, aECP + nt);
   h->sys = {nrAtoms, geometry, h->shellsECP.data(), h->KECP.data(), h->lECP.data(), h->nECP.data(),
             h->dECP.data(), h->aECP.data(), shellsBS, lBS, KBS, dBS, aBS, largeGridOrder,
-            tolerance, accuracy, n};
+            tolerance, accuracy, n, nullptr, 0};
+  if (shellOrdering) {  // triples of shells 0..lmax (src/libecp.c:159-165)
+    if (lmax < 0 || lmax > 24) {
+      ecpgb::set_error("lmax %d out of range for shellOrdering", lmax);
+      delete h;
+      return nullptr;
+    }
+    h->ordering.assign(shellOrdering, shellOrdering + 3 * ((lmax + 1) * (lmax + 2) * (lmax + 3) / 6));
+    h->sys.shellOrdering = h->ordering.data();
+    h->sys.orderingLmax = lmax;
+  }
   ecpgb::Parsed P;
   if (ecpgb::parse_system(h->sys, P)) {
     delete h;

@@ -63,7 +63,7 @@ void shift_pair(int deriv, int s, int &shifta, int &shiftb) {
 // The derivative scheme sizes every table for basis l up to maxLBS + n
 // (src/libecp.c:144-147): the tables of a job whose largest shell is shifted.
 TableKey table_key(const Parsed &P) {
-  return {P.maxLECP, P.maxLBS + P.deriv, P.largeGridOrder, P.tol, P.acc};
+  return {P.maxLECP, P.maxLBS + P.deriv, P.largeGridOrder, P.tol, P.acc, P.ordering};
 }
 
 void shift_block_l(int deriv, int la, int lb, int shifta, int shiftb, int &lpa, int &lpb) {
@@ -143,6 +143,28 @@ int parse_system(const ecpgb_system &s, Parsed &P) {
   }
   P.deriv = s.derivative;
   P.nShift = shift_count(P.deriv);
+  if (s.shellOrdering) {
+    // src/libecp.c:159: the order must reach maxLambda + maxAlpha + 1
+    const int need = P.maxLECP + 2 * (P.maxLBS + P.deriv);
+    if (s.orderingLmax < need) {
+      set_error("shellOrdering covers l <= %d; this job needs l <= %d", s.orderingLmax, need);
+      return 1;
+    }
+    const int lmax = s.orderingLmax;
+    if (lmax > 24) { set_error("orderingLmax %d too large", lmax); return 1; }
+    P.ordering.assign(s.shellOrdering, s.shellOrdering + 3 * ncum(lmax));
+    for (int l = 0; l <= lmax; l++) {  // each shell a permutation of its exponent triples
+      std::vector<char> seen((size_t)(l + 1) * (l + 1), 0);
+      for (int c = 0; c < ncart(l); c++) {
+        const int *e = &P.ordering[3 * (ncum(l - 1) + c)];
+        if (e[0] < 0 || e[1] < 0 || e[2] < 0 || e[0] + e[1] + e[2] != l || seen[e[0] * (l + 1) + e[1]]) {
+          set_error("shellOrdering: shell l = %d is not an order of its Cartesian functions", l);
+          return 1;
+        }
+        seen[e[0] * (l + 1) + e[1]] = 1;
+      }
+    }
+  }
   if (P.maxLBS + P.deriv > kMaxLBasis) {  // the shifted shells must fit the tables
     set_error("basis l %d with derivative order %d: shifted l above %d", P.maxLBS, P.deriv, kMaxLBasis);
     return 1;

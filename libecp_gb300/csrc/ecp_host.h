@@ -23,6 +23,7 @@ struct Parsed {
   // pair nShift times (pair-major, shift-minor, the reference's callback
   // order), pairShift the shift index of each entry
   int deriv = 0, nShift = 1;
+  std::vector<int> ordering;  // a caller's Cartesian order (empty: libint's)
   double tol = 1e-12, acc = 1e-14;
   std::vector<double> geom, primA, primD, termN, termD, termA;
   std::vector<int> shL, shK, shP, shAtom, shAO, shLocal, atomMaxL, atomShell0;

@@ -363,6 +363,17 @@ void build_tables(const TableKey &key, HostTables &t) {
     return;
   }
   cart_tables(t.tmDim, t.ijk, t.ijkIndex);
+  if (!key.ordering.empty()) {  // the caller's order within each shell (src/libecp.c:159-165)
+    if (key.ordering.size() < t.ijk.size()) {
+      t.status = 3;
+      return;
+    }
+    const int d = t.tmDim + 1;
+    for (size_t k = 0; k < t.ijk.size() / 3; k++) {
+      for (int c = 0; c < 3; c++) t.ijk[3 * k + c] = key.ordering[3 * k + c];
+      t.ijkIndex[(t.ijk[3 * k] * d + t.ijk[3 * k + 1]) * d + t.ijk[3 * k + 2]] = (int)k;
+    }
+  }
   cart2sph(t.tmDim, t.ijk, t.fac, t.cart2sph);
   poly2sph(t.cart2sph, t.tmDim, t.ijk, t.dfac, t.poly2sph);
   grid_ps93(128, t.xs, t.ws);

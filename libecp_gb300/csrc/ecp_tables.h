@@ -41,10 +41,13 @@ struct Schedule {
 struct TableKey {
   int maxLECP, maxLBS, largeGridOrder;
   double tolerance, accuracy;
+  // a caller's Cartesian order (libECP_init's shellOrdering): exponent
+  // triples of shells l = 0, 1, ... in the caller's order; empty = libint's
+  std::vector<int> ordering;
   // the tables do not depend on the quadrature tolerance
   bool operator==(const TableKey &o) const {
     return maxLECP == o.maxLECP && maxLBS == o.maxLBS && largeGridOrder == o.largeGridOrder &&
-           accuracy == o.accuracy;
+           accuracy == o.accuracy && ordering == o.ordering;
   }
 };
 

@@ -47,6 +47,10 @@ class EcpSystem:
     name: str = field(default="system")
     # nuclear-derivative order of libECP_init (0, 1, 2): blocks of shifted shells
     derivative: int = 0
+    # libECP_init's shellOrdering: Cartesian exponent triples of shells
+    # l = 0..ordering_lmax in the caller's order (None: libint's)
+    ordering: np.ndarray | None = None
+    ordering_lmax: int = 0
 
     def __post_init__(self):
         self.geometry = np.ascontiguousarray(self.geometry, dtype=np.float64).reshape(-1)

@@ -153,6 +153,8 @@ def ref_lib(path=REF_SO):
         lib.getIntegrals.restype = ct.c_int
         lib.ref_blocks_deriv.argtypes = _sys_argtypes() + [ct.c_int, ct.c_int, _I, ct.c_longlong, _D, _I,
                                                            ct.POINTER(ct.c_longlong)]
+        lib.ref_blocks_ordered.argtypes = _sys_argtypes() + [ct.c_int, _I, ct.c_int, _I, ct.c_longlong, _D,
+                                                             _I, ct.POINTER(ct.c_longlong)]
         _ref[path] = lib
     return _ref[path]
 
@@ -183,6 +185,22 @@ def ref_blocks_deriv(s, n, path=REF_SO):
     rc = lib.ref_blocks_deriv(*_sys_args(s), int(n), mb, meta.ctypes.data_as(_I), md,
                               data.ctypes.data_as(_D), ct.byref(nb), ct.byref(nd))
     return rc, meta[:10 * nb.value].reshape(-1, 10).copy(), data[:nd.value].copy()
+
+
+def ref_blocks_ordered(s, lmax, ordering, path=REF_SO):
+    """The reference's blocks in a caller's Cartesian order (libECP_init's
+    lmax and shellOrdering)."""
+    lib = ref_lib(path)
+    mb, md = _capacity(s, None)
+    meta = np.zeros(8 * mb, dtype=np.int32)
+    data = np.zeros(md, dtype=np.float64)
+    order = np.ascontiguousarray(ordering, dtype=np.int32)
+    nb = ct.c_int(0)
+    nd = ct.c_longlong(0)
+    rc = lib.ref_blocks_ordered(*_sys_args(s), int(lmax), order.ctypes.data_as(_I), mb,
+                                meta.ctypes.data_as(_I), md, data.ctypes.data_as(_D), ct.byref(nb),
+                                ct.byref(nd))
+    return rc, meta[:8 * nb.value].reshape(-1, 8).copy(), data[:nd.value].copy()
 
 
 def ref_matrix(s, path=REF_SO):

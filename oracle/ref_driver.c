@@ -141,3 +141,28 @@ int ref_blocks_deriv(int nrAtoms, double *geometry, int *shellsECP, int *KECP,
   return st;
 }
 
+/* The blocks of derivative order 0 in a caller's Cartesian order
+ * (libECP_init's lmax and shellOrdering, src/libecp.c:159-165); recorded as
+ * ref_blocks does. */
+int ref_blocks_ordered(int nrAtoms, double *geometry, int *shellsECP, int *KECP,
+                       int *lECP, double *nECP, double *dECP, double *aECP,
+                       int *shellsBS, int *lBS, int *KBS, double *dBS, double *aBS,
+                       int largeGridOrder, double tolerance, double accuracy,
+                       int lmax, int *ordering,
+                       int maxBlocks, int *meta, long long maxData, double *data,
+                       int *nBlocks, long long *nData) {
+  Recorder r;
+  memset(&r, 0, sizeof r);
+  r.maxBlocks = maxBlocks; r.meta = meta; r.maxData = maxData; r.data = data;
+  libECPHandle *h = libECP_init(nrAtoms, geometry, shellsECP, lECP, KECP, nECP,
+                                dECP, aECP, shellsBS, lBS, KBS, dBS, aBS, 0, lmax,
+                                ordering, largeGridOrder, tolerance, accuracy);
+  if (h == NULL) return -1;
+  int st = calculateECPIntegrals(h, record_block, &r);
+  libECP_free(h);
+  *nBlocks = r.nBlocks;
+  *nData = r.nData;
+  if (r.overflow) return -2;
+  return st;
+}
+

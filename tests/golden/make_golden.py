@@ -14,7 +14,9 @@ keeps the reference's table reads in bounds and adds exactly zero; the blocks
 are those of the unpadded system.  The example-like fixture also stores the
 reference's getIntegrals matrix.
 
-The deriv*_ fixtures hold the nuclear-derivative blocks of libECP_init's
+The ordered_* fixtures hold blocks in a caller's Cartesian order
+(libECP_init's lmax and shellOrdering; here libint's order reversed within
+each shell).  The deriv*_ fixtures hold the nuclear-derivative blocks of libECP_init's
 order n (1 or 2): meta rows (A, s1, la, shifta, B, s2, lb, shiftb, C, type).
 Their systems keep basis l + n below the ECP's L, where the reference's
 tables stay in bounds without padding.
@@ -56,6 +58,39 @@ DERIV_CASES = {
 }
 
 
+def reversed_ordering(lmax):
+    """libint's Cartesian order with every shell reversed."""
+    from libecp_gb300 import libint_ordering
+    from libecp_gb300.workloads import ncart
+    d = libint_ordering(lmax)
+    out, off = [], 0
+    for l in range(lmax + 1):
+        out.append(d[off:off + 3 * ncart(l)].reshape(-1, 3)[::-1].ravel())
+        off += 3 * ncart(l)
+    return np.concatenate(out).astype(np.int32)
+
+
+# blocks in a caller's Cartesian order (libECP_init's lmax, shellOrdering)
+ORDERED_CASES = {
+    "ordered_rev_s2": lambda: W.random_system(2, n_atoms=3, n_centres=2, lmax_basis=2, lmax_ecp=3),
+}
+
+
+def save_ordered(name, s):
+    lmax = s.max_l_ecp() + 2 * s.max_l_basis()
+    order = reversed_ordering(lmax)
+    rc, meta, data = O.ref_blocks_ordered(s, lmax, order)
+    if rc != 0:
+        raise RuntimeError(f"reference failed on {name}: {rc}")
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"), geometry=s.geometry, shellsECP=s.shellsECP,
+        KECP=s.KECP, lECP=s.lECP, nECP=s.nECP, dECP=s.dECP, aECP=s.aECP, shellsBS=s.shellsBS,
+        lBS=s.lBS, KBS=s.KBS, dBS=s.dBS, aBS=s.aBS,
+        params=np.array([s.largeGridOrder, s.tolerance, s.accuracy]), ordering=order,
+        ordering_lmax=np.array(lmax), padded=np.array(False), meta=meta, data=data)
+    print(f"{name}: ordering lmax={lmax}, {len(meta)} blocks, max|I|={np.abs(data).max():.3e}")
+
+
 def save_deriv(name, n, s):
     assert s.max_l_basis() + n < s.max_l_ecp()
     rc, meta, data = O.ref_blocks_deriv(s, n)
@@ -95,6 +130,9 @@ def load(path) -> tuple:
                     z["aECP"], z["shellsBS"], z["lBS"], z["KBS"], z["dBS"], z["aBS"],
                     int(p[0]), float(p[1]), float(p[2]), name=os.path.basename(path),
                     derivative=int(z["derivative"]) if "derivative" in z.files else 0)
+    if "ordering" in z.files:
+        s.ordering = z["ordering"]
+        s.ordering_lmax = int(z["ordering_lmax"])
     return s, z
 
 
@@ -104,6 +142,8 @@ if __name__ == "__main__":
         save(name, make())
     for name, (n, make) in DERIV_CASES.items():
         save_deriv(name, n, make())
+    for name, make in ORDERED_CASES.items():
+        save_ordered(name, make())
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         gcc = subprocess.run(["gcc", "--version"], capture_output=True, text=True).stdout.splitlines()[0]
         libc = " ".join(platform.libc_ver())

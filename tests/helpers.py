@@ -13,8 +13,14 @@ TOL_ABS = 1e-10
 
 
 def golden_files():
-    """Fixtures of derivative order 0."""
-    return sorted(f for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and not f.startswith("deriv"))
+    """Fixtures of derivative order 0 in libint's Cartesian order."""
+    return sorted(f for f in os.listdir(GOLDEN_DIR)
+                  if f.endswith(".npz") and not f.startswith(("deriv", "ordered")))
+
+
+def ordered_golden_files():
+    """Fixtures in a caller's Cartesian order (libECP_init's shellOrdering)."""
+    return sorted(f for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and f.startswith("ordered"))
 
 
 def deriv_golden_files():

@@ -39,3 +39,14 @@ def test_reference_reproduces_fixture(name):
     rc, meta, data = O.ref_blocks_deriv(s, s.derivative)
     assert rc == 0
     assert np.array_equal(meta, z["meta"]) and np.array_equal(data, z["data"])
+
+
+def test_ordered_fixture_reproduced_by_reference():
+    from oracle import oracle as O
+    from tests.helpers import ordered_golden_files
+    if not O.ref_available():
+        pytest.skip("reference build not present on this machine")
+    for name in ordered_golden_files():
+        s, z = load_golden(name)
+        rc, meta, data = O.ref_blocks_ordered(s, s.ordering_lmax, s.ordering)
+        assert rc == 0 and np.array_equal(meta, z["meta"]) and np.array_equal(data, z["data"])
