@@ -102,6 +102,19 @@ int ecpgb_blocks(const ecpgb_system *s, int mode, double *values, long long *off
 int ecpgb_getIntegrals(const ecpgb_system *s, int mode, int rowdim, double *I,
                        ecpgb_info *info);
 
+/* Blocks in real spherical harmonics: both blocks of every emitted unit as
+ * T(la) B T(lb)^T, T the reference's Cartesian -> real spherical matrices
+ * (src/transformations.c:29-87, Schlegel and Frisch; rows m = -l..l) in the
+ * job's Cartesian order, computed on the GPU.  T assumes Cartesian functions
+ * each normalised on its own, so the caller's contraction coefficients must
+ * carry those norms for the result to be the spherical functions' integrals.
+ * Layout as ecpgb_blocks with 2 (2 la + 1)(2 lb + 1) values per unit
+ * (ecpgb_layout_sph gives the sizes); ecpgb_cart2sph gives T(l),
+ * (2l+1) x ncart(l), libint order.  No host CPU transform. */
+int ecpgb_layout_sph(const ecpgb_system *s, long long *nUnits, long long *nValues);
+int ecpgb_blocks_sph(const ecpgb_system *s, int mode, double *values, long long *offsets, int *status);
+int ecpgb_cart2sph(int l, double *out);
+
 /* Device-side consumers of the blocks.  With a symmetric density matrix D
  * (dim x dim, row stride ldD, the Cartesian AO order of getIntegrals):
  * *energy = sum_{mu nu} D_{mu nu} V_{mu nu} of the ECP matrix V, and

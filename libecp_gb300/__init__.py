@@ -136,6 +136,12 @@ def lib() -> ct.CDLL:
     L.ecpgb_server_get_stats.restype = ct.c_int
     L.ecpgb_server_free.argtypes = [ct.c_void_p]
     L.ecpgb_server_free.restype = None
+    L.ecpgb_layout_sph.argtypes = [P, _LL, _LL]
+    L.ecpgb_layout_sph.restype = ct.c_int
+    L.ecpgb_blocks_sph.argtypes = [P, ct.c_int, _D, _LL, _I]
+    L.ecpgb_blocks_sph.restype = ct.c_int
+    L.ecpgb_cart2sph.argtypes = [ct.c_int, _D]
+    L.ecpgb_cart2sph.restype = ct.c_int
     L.ecpgb_gradient.argtypes = [P, ct.c_int, _D, ct.c_int, _D, _D]
     L.ecpgb_gradient.restype = ct.c_int
     L.ecpgb_load_system.argtypes = [ct.c_char_p, ct.c_char_p, ct.c_char_p]
@@ -555,4 +561,44 @@ def gradient(s: EcpSystem, D: np.ndarray, mode: int = ECPGB_FP64):
                             g.ctypes.data_as(_D)):
         raise RuntimeError(f"ecpgb_gradient failed: {last_error()}")
     return e.value, g
+
+
+def cart2sph(l: int) -> np.ndarray:
+    """The reference's Cartesian -> real spherical matrix T(l), (2l+1) x ncart(l)."""
+    out = np.zeros((2 * l + 1, ncart(l)))
+    if lib().ecpgb_cart2sph(int(l), out.ctypes.data_as(_D)):
+        raise RuntimeError(last_error())
+    return out
+
+
+def blocks_sph(s: EcpSystem, mode: int = ECPGB_FP64):
+    """Every emitted block in real spherical harmonics (ecpgb_blocks_sph), in
+    the reference's callback order: (meta, data) as blocks() / blocks_deriv()."""
+    L = lib()
+    cs = c_system(s)
+    nu, nv = ct.c_longlong(0), ct.c_longlong(0)
+    if L.ecpgb_layout_sph(ct.byref(cs), ct.byref(nu), ct.byref(nv)):
+        raise RuntimeError(last_error())
+    vals = np.zeros(max(nv.value, 1))
+    offs = np.zeros(max(nu.value, 1), dtype=np.int64)
+    st = np.zeros(max(nu.value, 1), dtype=np.int32)
+    if L.ecpgb_blocks_sph(ct.byref(cs), mode, vals.ctypes.data_as(_D), offs.ctypes.data_as(_LL),
+                          st.ctypes.data_as(_I)):
+        raise RuntimeError(f"ecpgb_blocks_sph failed: {last_error()}")
+    n = int(getattr(s, "derivative", 0))
+    shifts = SHIFTS[n]
+    meta, data = [], []
+    for i, (A, s1, la, B, s2, lb, C) in enumerate(unit_table(s)):
+        for k, (ha, hb) in enumerate(shifts):
+            u = i * len(shifts) + k
+            if st[u] == UNIT_SKIPPED:
+                continue
+            lpa, lpb = block_l(n, la, lb, ha, hb)
+            m = (2 * lpa + 1) * (2 * lpb + 1)
+            o = int(offs[u])
+            for t in (1, 2):
+                meta.append((A, s1, la, ha, B, s2, lb, hb, C, t) if n else (A, s1, la, B, s2, lb, C, t))
+                data.append(vals[o + (t - 1) * m:o + t * m])
+    meta = np.array(meta, dtype=np.int32).reshape(-1, 10 if n else 8)
+    return meta, (np.concatenate(data) if data else np.zeros(0))
 

@@ -194,6 +194,17 @@ int ecpgb_blocks(const ecpgb_system *s, int mode, double *values, long long *off
   return ecpgb::run_blocks(*s, mode, values, offsets, status, info, nullptr) ? 1 : 0;
 }
 
+int ecpgb_layout_sph(const ecpgb_system *s, long long *nUnits, long long *nValues) {
+  return s ? ecpgb::layout_sph(*s, nUnits, nValues) : 1;
+}
+
+int ecpgb_blocks_sph(const ecpgb_system *s, int mode, double *values, long long *offsets, int *status) {
+  if (!s) { ecpgb::set_error("null system"); return 1; }
+  return ecpgb::run_blocks_sph(*s, mode, values, offsets, status);
+}
+
+int ecpgb_cart2sph(int l, double *out) { return out ? ecpgb::cart2sph_table(l, out) : 1; }
+
 int ecpgb_gradient(const ecpgb_system *s, int mode, const double *D, int ldD, double *energy, double *grad) {
   if (!s || !D) { ecpgb::set_error("null system or density matrix"); return 1; }
   return ecpgb::run_gradient(*s, mode, D, ldD, energy, grad);

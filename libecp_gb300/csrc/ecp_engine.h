@@ -160,6 +160,10 @@ inline void record_timing(cudaEvent_t e, cudaStream_t st) {
 // the energy of the upper-triangle AO matrix V.
 void launch_gradient(const DevJob &J, const double *D, int ldD, double *grad, cudaStream_t st);
 void launch_energy(const double *V, int dim, const double *D, int ldD, double *E, cudaStream_t st);
+// Both blocks of every emitted unit in real spherical harmonics (sphOff per
+// pair entry within a centre, sphStride values per centre).
+void launch_to_sph(const DevJob &J, const double *c2s, const long long *sphOff, long long sphStride,
+                   double *sout, cudaStream_t st);
 
 // Launchers return 0, 3 when the shared memory does not fit, or
 // kLaunchErrorBase + the cudaError_t of a failed launch.

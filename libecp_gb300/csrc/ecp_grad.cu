@@ -115,6 +115,51 @@ __global__ void __launch_bounds__(1024) k_energy(const double *V, int dim, const
   if (threadIdx.x == 0) *E = part[0];
 }
 
+// Real-spherical blocks: S = T(la) B T(lb)^T for both blocks of every
+// emitted unit, T the Cartesian -> real spherical matrices of
+// src/transformations.c:29-87 ([l][m][c] blocks, in the job's Cartesian
+// order).  One CTA per unit; sphOff / sphStride the spherical layout.
+__global__ void __launch_bounds__(64) k_to_sph(DevJob J, const double *c2s, const long long *sphOff,
+                                               long long sphStride, double *sout) {
+  __shared__ double tmp[2 * 15 * 15];
+  const long long u = blockIdx.x;
+  if (J.status[u] == kUnitSkipped) return;
+  const int c = (int)(u / J.nPairs), px = (int)(u % J.nPairs);
+  const UnitShift sh = unit_shift(J, px, J.shL[J.pairA[px]], J.shL[J.pairB[px]], 0, 1, 2);
+  const int la = sh.lpa, lb = sh.lpb, na = NCART(la), nb = NCART(lb), ma = 2 * la + 1, mb = 2 * lb + 1;
+  auto off = [](int l) {
+    int o = 0;
+    for (int k = 0; k < l; k++) o += (2 * k + 1) * NCART(k);
+    return o;
+  };
+  const double *Ta = c2s + off(la), *Tb = c2s + off(lb);
+  const double *src = J.out + (size_t)c * J.centreStride + J.pairOff[px];
+  double *dst = sout + (size_t)c * sphStride + sphOff[px];
+  for (int t = 0; t < 2; t++) {
+    const double *B = src + t * na * nb;
+    for (int e = threadIdx.x; e < ma * nb; e += blockDim.x) {  // T(la) B
+      const int m = e / nb, j = e % nb;
+      double v = 0.0;
+      for (int i = 0; i < na; i++) v += Ta[m * na + i] * B[i * nb + j];
+      tmp[e] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ma * mb; e += blockDim.x) {  // (T(la) B) T(lb)^T
+      const int m = e / mb, n = e % mb;
+      double v = 0.0;
+      for (int j = 0; j < nb; j++) v += tmp[m * nb + j] * Tb[n * nb + j];
+      dst[t * ma * mb + e] = v;
+    }
+    __syncthreads();
+  }
+}
+
+void launch_to_sph(const DevJob &J, const double *c2s, const long long *sphOff, long long sphStride,
+                   double *sout, cudaStream_t st) {
+  const long long n = (long long)J.nCentres * J.nPairs;
+  if (n > 0) k_to_sph<<<(unsigned)n, 64, 0, st>>>(J, c2s, sphOff, sphStride, sout);
+}
+
 void launch_gradient(const DevJob &J, const double *D, int ldD, double *grad, cudaStream_t st) {
   const long long warps = (long long)J.nCentres * (J.nPairs / 4);
   if (warps <= 0) return;

@@ -213,7 +213,7 @@ struct DevTables {
   TableKey key{};
   HostTables host;
   DBuf<float> besHf;
-  DBuf<double> xs, ws, xl, wl, besT, besC, besH, besA, shNorm, p2s, fac, dfac, omega;
+  DBuf<double> xs, ws, xl, wl, besT, besC, besH, besA, shNorm, p2s, fac, dfac, omega, c2s;
   DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items;
   int nItemsMax = 0;
 };
@@ -273,6 +273,7 @@ struct Engine {
               t->fac.upload(h.fac, stream) && t->dfac.upload(h.dfac, stream) &&
               t->omega.upload(h.omega, stream) && t->ijk.upload(h.ijk, stream) &&
               t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) && t->besA.upload(h.besselA, stream) && t->besHf.upload(h.besselHf, stream) &&
+              t->c2s.upload(h.cart2sph, stream) &&
               t->shNorm.upload(h.shNorm, stream);
     // used-triple lists per (la, lb, l)
     int LB = h.maxLBS, LE = h.maxLECP > 0 ? h.maxLECP : 1;
@@ -698,6 +699,84 @@ int run_gradient(const ecpgb_system &s0, int mode, const double *D, int ldD, dou
     cudaError_t ce = cudaStreamSynchronize(E.stream);
     if (ce != cudaSuccess) { set_error("device error: %s", cudaGetErrorString(ce)); return 1; }
   }
+  return 0;
+}
+
+// Spherical layout of the blocks: per pair entry 2 nsph(lpa) nsph(lpb)
+// values (lpa, lpb the l of the blocks the entry hands out).
+static long long sph_layout(const Parsed &P, std::vector<long long> &off) {
+  off.assign(P.nPairs, 0);
+  long long o = 0;
+  for (int px = 0; px < P.nPairs; px++) {
+    off[px] = o;
+    int la = P.shL[P.pairA[px]], lb = P.shL[P.pairB[px]], ha = 0, hb = 0, lpa = la, lpb = lb;
+    if (P.deriv) {
+      shift_pair(P.deriv, P.pairShift[px], ha, hb);
+      if (la + ha < 0 || lb + hb < 0) continue;
+      shift_block_l(P.deriv, la, lb, ha, hb, lpa, lpb);
+    }
+    o += 2LL * (2 * lpa + 1) * (2 * lpb + 1);
+  }
+  return o;
+}
+
+int layout_sph(const ecpgb_system &s, long long *nUnits, long long *nValues) {
+  Parsed P;
+  if (parse_system(s, P)) return 1;
+  std::vector<long long> off;
+  const long long stride = sph_layout(P, off);
+  if (nUnits) *nUnits = (long long)P.nCentres * P.nPairs;
+  if (nValues) *nValues = (long long)P.nCentres * stride;
+  return 0;
+}
+
+// Every block in real spherical harmonics (src/transformations.c:29-87),
+// transformed on the GPU; the ecpgb_blocks contract otherwise.
+int run_blocks_sph(const ecpgb_system &s, int mode, double *values, long long *offsets, int *status) {
+  Engine &E = engine();
+  std::unique_lock<std::mutex> lk(E.mu);
+  if (!valid_mode(mode)) { set_error("unknown mode %d", mode); return 1; }
+  if (E.ensure_init()) return 1;
+  Parsed P;
+  if (parse_system(s, P)) return 1;
+  const long long nUnits = (long long)P.nCentres * P.nPairs;
+  if (nUnits == 0) return 0;
+  const DevTables *T = E.get_tables(table_key(P));
+  if (!T || E.use_schedules(T, &lk)) return 1;
+  JobBuffers &B = E.shared;
+  DevJob J;
+  if (stage_job(P, T, B, J, mode, E.stream)) return 1;
+  std::vector<long long> off;
+  const long long stride = sph_layout(P, off);
+  const size_t nv = (size_t)P.nCentres * stride;
+  if (!B.sphOff.ensure(off.size() + 1) || !B.sout.ensure(nv + 1)) {
+    set_error("device allocation failed");
+    return 1;
+  }
+  CUDA_OK(cudaMemcpyAsync(B.sphOff.p, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice, E.stream));
+  CUDA_OK(cudaMemsetAsync(B.sout.p, 0, sizeof(double) * nv, E.stream));
+  if (run_pipeline(B, J, mode, nullptr, nullptr, nullptr, E.stream)) return 1;
+  launch_to_sph(J, T->c2s.p, B.sphOff.p, stride, B.sout.p, E.stream);
+  if (values) CUDA_OK(cudaMemcpyAsync(values, B.sout.p, sizeof(double) * nv, cudaMemcpyDeviceToHost, E.stream));
+  std::vector<int> st(nUnits);
+  CUDA_OK(cudaMemcpyAsync(st.data(), B.status.p, sizeof(int) * nUnits, cudaMemcpyDeviceToHost, E.stream));
+  cudaError_t ce = cudaStreamSynchronize(E.stream);
+  if (ce != cudaSuccess) { set_error("device error: %s", cudaGetErrorString(ce)); return 1; }
+  for (long long u = 0; u < nUnits; u++) {
+    if (status) status[u] = st[u];
+    if (offsets) offsets[u] = (u / P.nPairs) * stride + off[u % P.nPairs];
+  }
+  return 0;
+}
+
+int cart2sph_table(int l, double *out) {
+  if (l < 0 || l > kMaxLBasis) { set_error("l %d outside 0..%d", l, kMaxLBasis); return 1; }
+  HostTables t;
+  build_tables({1, kMaxLBasis, 1024, 1e-12, 1e-14, {}}, t);
+  if (t.status) { set_error("table build failed"); return 1; }
+  size_t o = 0;
+  for (int k = 0; k < l; k++) o += (size_t)(2 * k + 1) * ncart(k);
+  std::memcpy(out, t.cart2sph.data() + o, sizeof(double) * (2 * l + 1) * ncart(l));
   return 0;
 }
 

@@ -99,6 +99,8 @@ struct JobBuffers {
   DBuf<double> radius, utab, uL, F, cgeo, usp, ang, out, mat;
   DBuf<int> gridEnd, win, status, err;
   DBuf<unsigned long long> head;
+  DBuf<double> sout;       // spherical blocks
+  DBuf<long long> sphOff;  // their per-entry offsets
   PinnedBuf pinned, pinnedOut;
   int *pinnedErr = nullptr;
   size_t smem = 0, smemFast = 0;
@@ -119,6 +121,9 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
                ecpgb_info *info, Parsed *parsedOut);
 int layout(const ecpgb_system &s, long long *nUnits, long long *nValues);
 int run_gradient(const ecpgb_system &s, int mode, const double *D, int ldD, double *energy, double *grad);
+int layout_sph(const ecpgb_system &s, long long *nUnits, long long *nValues);
+int run_blocks_sph(const ecpgb_system &s, int mode, double *values, long long *offsets, int *status);
+int cart2sph_table(int l, double *out);
 void *job_create(const ecpgb_system &s, int mode);
 int job_run(void *j, int nRuns, int flushL2, float *msRun, float *msUnit);
 int job_matrix(void *j, int rowdim, double *I);
