@@ -146,10 +146,11 @@ void ecpgb_job_free(ecpgb_job *j);
  * gcap: width cap of the type-1 step table in doubles per slot, which sets
  * the primitive pairs per warp and the CTAs per SM; balance: 1 = a unit with
  * few primitive pairs gets narrower type-1 groups so that all its warps
- * work.  msUnit: the unit kernel's time when the autotuner measured it, else
- * 0. */
+ * work; screen: 1 = with the queue launch, a screening stage first compacts
+ * the queue to the units that compute blocks.  msUnit: the unit kernel's
+ * time when the autotuner measured it, else 0. */
 typedef struct {
-  int queue, sorted, gcap, balance;
+  int queue, sorted, gcap, balance, screen;
   float msUnit;
 } ecpgb_launch_config;
 

@@ -50,7 +50,7 @@ class EcpgbInfo(ct.Structure):
 class LaunchConfig(ct.Structure):
     """ecpgb_launch_config: batched-path launch configuration."""
     _fields_ = [("queue", ct.c_int), ("sorted", ct.c_int), ("gcap", ct.c_int), ("balance", ct.c_int),
-                ("msUnit", ct.c_float)]
+                ("screen", ct.c_int), ("msUnit", ct.c_float)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -396,17 +396,18 @@ class Job:
             raise RuntimeError(f"ecpgb_job_tune failed ({rc}): {last_error()}")
         return chosen.as_dict(), [trials[i].as_dict() for i in range(n.value)]
 
-    def config(self, queue=None, sorted=None, gcap=None, balance=None) -> dict:
+    def config(self, queue=None, sorted=None, gcap=None, balance=None, screen=None) -> dict:
         """Reads the launch configuration; sets the fields given."""
         cur = LaunchConfig()
         if lib().ecpgb_job_config(self._h, None, ct.byref(cur)):
             raise RuntimeError(last_error())
-        if queue is None and sorted is None and gcap is None and balance is None:
+        if all(v is None for v in (queue, sorted, gcap, balance, screen)):
             return cur.as_dict()
         new = LaunchConfig(cur.queue if queue is None else int(queue),
                            cur.sorted if sorted is None else int(sorted),
                            cur.gcap if gcap is None else int(gcap),
-                           cur.balance if balance is None else int(balance), 0.0)
+                           cur.balance if balance is None else int(balance),
+                           cur.screen if screen is None else int(screen), 0.0)
         if lib().ecpgb_job_config(self._h, ct.byref(new), ct.byref(cur)):
             raise RuntimeError(last_error())
         return cur.as_dict()

@@ -92,6 +92,10 @@ struct DevJob {
   int gcap;                      // type-1 step-table width cap (doubles per slot per warp)
   int mixed;                     // 1: FP32 Bessel Taylor rows and ECP channel terms
   int balance;                   // 1: type-1 groups narrowed so that every warp gets pairs
+  // screening stage (batched path): the queue of units that compute blocks
+  int *live;                     // live units in queue order (null: no screening stage)
+  unsigned long long *liveCount; // their number
+  int *screenBlocks;             // per-CTA counts, then offsets, of the screening kernels
 };
 
 // Launch configuration of the batched path (picked by the autotuner).
@@ -101,6 +105,7 @@ struct FastConfig {
   int gcap = 45;   // type-1 step-table width cap; smaller caps fit more CTAs per SM
   int mixed = 0;   // set from the job's mode (ECPGB_MIXED), not tuned
   int balance = 1; // narrower type-1 groups when a unit has few primitive pairs
+  int screen = 1;  // with the queue launch: a screening stage compacts the queue to live units
 };
 
 // Shared-memory layout of the unit kernel (offsets in doubles).

@@ -973,6 +973,9 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   }
 }
 
+// The unit at queue position i (cost order, or the reference's order).
+__device__ inline long long queue_unit(const DevJob &J, long long i) { return J.order ? J.order[i] : i; }
+
 // A CTA per unit; blockIdx.x is a queue position.
 __global__ void __launch_bounds__(kUnitThreads) k_unit_fast(DevJob J) {
   extern __shared__ double sm[];
@@ -988,15 +991,81 @@ __global__ void __launch_bounds__(kUnitThreads) k_unit_queue(DevJob J) {
   extern __shared__ double sm[];
   __shared__ FastShared S;
   __shared__ long long next;
-  const long long n = (long long)J.nCentres * J.nPairs;
+  // with the screening stage the queue holds the live units only
+  const long long n = J.live ? (long long)*J.liveCount : (long long)J.nCentres * J.nPairs;
   for (;;) {
     if (threadIdx.x == 0) next = (long long)atomicAdd(J.queueHead, 1ull);
     __syncthreads();
     const long long i = next;
     if (i >= n) break;
-    unit_fast(J, J.order ? (long long)J.order[i] : i, S, sm);
+    unit_fast(J, J.live ? (long long)J.live[i] : queue_unit(J, i), S, sm);
     __syncthreads();  // shared state is rewritten by the next unit
   }
+}
+
+// ---------------------------------------------------------- screening stage
+
+// True when unit u computes blocks: the unit kernels' own early exits (the
+// screened windows of src/libecp.c:296-330 and the derivative skip rules).
+static __device__ bool unit_live(const DevJob &J, long long u) {
+  const int c = (int)(u / J.nPairs), pr = (int)(u % J.nPairs);
+  const int sa = J.pairA[pr], sb = J.pairB[pr];
+  const int *wa = J.win + ((size_t)c * J.nShells + sa) * 3;
+  const int *wb = J.win + ((size_t)c * J.nShells + sb) * 3;
+  const UnitShift sh = unit_shift(J, pr, J.shL[sa], J.shL[sb], J.shAtom[sa], J.shAtom[sb], J.ctrAtom[c]);
+  if (wa[2] || wb[2] || sh.skip) return false;
+  return (wa[0] > wb[0] ? wa[0] : wb[0]) < (wa[1] > wb[1] ? wa[1] : wb[1]);
+}
+
+constexpr int kScreenThreads = 256;
+
+// Live units per CTA chunk of the queue.
+__global__ void __launch_bounds__(kScreenThreads) k_screen_count(DevJob J, long long n) {
+  const long long i = (long long)blockIdx.x * kScreenThreads + threadIdx.x;
+  const int live = i < n && unit_live(J, queue_unit(J, i));
+  const int cnt = __syncthreads_count(live);
+  if (threadIdx.x == 0) J.screenBlocks[blockIdx.x] = cnt;
+}
+
+// Exclusive scan of the per-CTA counts (one CTA); the total is the live count.
+__global__ void __launch_bounds__(1024) k_screen_scan(DevJob J, int nBlocks) {
+  __shared__ int v[1024];
+  __shared__ long long base;
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  for (int b0 = 0; b0 < nBlocks; b0 += 1024) {
+    const int b = b0 + threadIdx.x;
+    const int x = b < nBlocks ? J.screenBlocks[b] : 0;
+    v[threadIdx.x] = x;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
+      const int y = threadIdx.x >= off ? v[threadIdx.x - off] : 0;
+      __syncthreads();
+      v[threadIdx.x] += y;
+      __syncthreads();
+    }
+    if (b < nBlocks) J.screenBlocks[b] = (int)(base + v[threadIdx.x] - x);
+    __syncthreads();
+    if (threadIdx.x == 1023) base += v[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *J.liveCount = (unsigned long long)base;
+}
+
+// Stable compaction of the live units; the others are marked skipped here.
+__global__ void __launch_bounds__(kScreenThreads) k_screen_scatter(DevJob J, long long n) {
+  __shared__ int warpCnt[kScreenThreads / 32];
+  const long long i = (long long)blockIdx.x * kScreenThreads + threadIdx.x;
+  const long long u = i < n ? queue_unit(J, i) : -1;
+  const bool live = u >= 0 && unit_live(J, u);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned m = __ballot_sync(0xffffffffu, live);
+  if (lane == 0) warpCnt[warp] = __popc(m);
+  __syncthreads();
+  int pos = J.screenBlocks[blockIdx.x] + __popc(m & ((1u << lane) - 1u));
+  for (int w = 0; w < warp; w++) pos += warpCnt[w];
+  if (live) J.live[pos] = (int)u;
+  else if (u >= 0) J.status[u] = kUnitSkipped;
 }
 
 __global__ void k_reset(int *errWord, unsigned long long *queueHead) {
@@ -1071,8 +1140,16 @@ int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, con
   Jc.mixed = cfg.mixed;
   Jc.balance = cfg.balance;
   if (!cfg.sorted) Jc.order = nullptr;
+  const bool screen = cfg.queue && cfg.screen && J.queueHead && J.live && J.liveCount && J.screenBlocks;
+  if (!screen) Jc.live = nullptr;
   launch_prologue(Jc, st);
   long long nUnits = (long long)J.nCentres * J.nPairs;
+  if (screen && nUnits > 0) {  // screening stage: the queue of live units
+    const long long nb = (nUnits + kScreenThreads - 1) / kScreenThreads;
+    k_screen_count<<<(unsigned)nb, kScreenThreads, 0, st>>>(Jc, nUnits);
+    k_screen_scan<<<1, 1024, 0, st>>>(Jc, (int)nb);
+    k_screen_scatter<<<(unsigned)nb, kScreenThreads, 0, st>>>(Jc, nUnits);
+  }
   if (u0) record_timing(u0, st);
   if (nUnits > 0) {
     if (cfg.queue && J.queueHead) {

@@ -510,6 +510,16 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.radius = B.radius.p; J.utab = B.utab.p; J.uL = B.uL.p; J.gridEnd = B.gridEnd.p; J.win = B.win.p;
   J.F = B.F.p; J.cgeo = B.cgeo.p; J.usp = B.usp.p; J.ang = B.ang.p; J.out = B.out.p;
   J.status = B.status.p; J.mat = B.mat.p; J.errWord = B.err.p; J.queueHead = B.head.p;
+  if (mode != ECPGB_FP64) {  // screening stage buffers of the batched path
+    const size_t nu = nc * (size_t)P.nPairs;
+    if (!B.live.ensure(nu + 1) || !B.screenBlocks.ensure(nu / 256 + 2) || !B.liveCount.ensure(1)) {
+      set_error("device allocation failed for the screening stage");
+      return -1;
+    }
+    J.live = B.live.p;
+    J.liveCount = B.liveCount.p;
+    J.screenBlocks = B.screenBlocks.p;
+  }
   J.gcap = FastConfig{}.gcap;
   J.besH = T->besH.p;
   J.besA = T->besA.p;
@@ -795,7 +805,7 @@ struct ResidentJob {
   const DevTables *T = nullptr;
   JobBuffers B;
   DevJob J;
-  int launches = 7;  // reset, four per-job stages, the unit kernel, the scatter
+
   int mode = ECPGB_FP64;
   FastConfig cfg;
   bool useGraph = true;
@@ -851,7 +861,7 @@ void *job_create(const ecpgb_system &s, int mode) {
   R->T = E.get_tables(table_key(R->P));
   if (!R->T || stage_job(R->P, R->T, R->B, R->J, mode, E.stream)) { delete R; return nullptr; }
   R->cfg = E.config_for(R->J.maxLBS, R->J.maxLECP);
-  R->launches = R->P.deriv ? 6 : 7;  // no AO scatter for derivative blocks
+
   // skipped units are never written: their values read as zero
   cudaMemsetAsync(R->B.out.p, 0, sizeof(double) * (size_t)R->P.nCentres * R->P.centreStride, E.stream);
   if (cudaStreamSynchronize(E.stream) != cudaSuccess) { set_error("staging failed"); delete R; return nullptr; }
@@ -915,7 +925,9 @@ int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
   return 0;
 }
 
-static ecpgb_launch_config to_c(const FastConfig &c, float ms) { return {c.queue, c.sorted, c.gcap, c.balance, ms}; }
+static ecpgb_launch_config to_c(const FastConfig &c, float ms) {
+  return {c.queue, c.sorted, c.gcap, c.balance, c.screen, ms};
+}
 
 int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials, int *nTrials) {
   Engine &E = engine();
@@ -939,6 +951,9 @@ int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials,
     for (int queue : {1, 0}) cand.push_back(mk(queue, 1, gcap, 1));
   cand.push_back(mk(0, 0, 45, 1));
   cand.push_back(mk(1, 1, 45, 0));
+  FastConfig noScreen = mk(1, 1, 45, 1);
+  noScreen.screen = 0;
+  cand.push_back(noScreen);
   const size_t flushBytes = 256u << 20;
   if (!E.flush.ensure(flushBytes)) { set_error("flush buffer allocation failed"); return 1; }
   cudaEvent_t u0, u1;
@@ -991,6 +1006,7 @@ int job_config(void *vj, const ecpgb_launch_config *cfg, ecpgb_launch_config *ou
     c.sorted = cfg->sorted ? 1 : 0;
     c.gcap = cfg->gcap;
     c.balance = cfg->balance ? 1 : 0;
+    c.screen = cfg->screen ? 1 : 0;
     if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap), c.queue) < 1) {
       set_error("configuration does not fit on an SM");
       return 1;
@@ -1051,7 +1067,14 @@ long long job_units(const void *vj, long long *emitted) {
   return n;
 }
 
-int job_launches(const void *vj) { return ((const ResidentJob *)vj)->launches; }
+int job_launches(const void *vj) {
+  // reset, four per-job stages, the unit kernel, the AO scatter (order 0), and
+  // with the batched queue launch the three screening kernels
+  const auto *R = (const ResidentJob *)vj;
+  int n = 6 + (R->P.deriv ? 0 : 1);
+  if (R->mode != ECPGB_FP64 && R->cfg.queue && R->cfg.screen) n += 3;
+  return n;
+}
 
 void job_free(void *vj) {
   Engine &E = engine();

@@ -98,7 +98,8 @@ struct JobBuffers {
   DBuf<char> in;
   DBuf<double> radius, utab, uL, F, cgeo, usp, ang, out, mat;
   DBuf<int> gridEnd, win, status, err;
-  DBuf<unsigned long long> head;
+  DBuf<unsigned long long> head, liveCount;
+  DBuf<int> live, screenBlocks;  // screening stage of the batched path
   DBuf<double> sout;       // spherical blocks
   DBuf<long long> sphOff;  // their per-entry offsets
   PinnedBuf pinned, pinnedOut;
@@ -109,7 +110,8 @@ struct JobBuffers {
   // device bytes held by the buffers
   size_t device_bytes() const {
     return in.cap + 8 * (radius.cap + utab.cap + uL.cap + F.cap + cgeo.cap + usp.cap + ang.cap + out.cap + mat.cap) +
-           4 * (gridEnd.cap + win.cap + status.cap + err.cap) + 8 * head.cap;
+           4 * (gridEnd.cap + win.cap + status.cap + err.cap + live.cap + screenBlocks.cap) +
+           8 * (head.cap + liveCount.cap);
   }
   ~JobBuffers() {
     if (pinnedErr) cudaFreeHost(pinnedErr);

@@ -34,12 +34,13 @@ def _run(eg, job, **cfg):
 
 def test_queue_order_and_graph_are_bitwise_neutral(eg, system):
     j = eg.Job(system, mode=eg.ECPGB_FAST)
-    base_v, base_s = _run(eg, j, queue=1, sorted=1, gcap=45)
-    for cfg in ({"queue": 0, "sorted": 1}, {"queue": 0, "sorted": 0}, {"queue": 1, "sorted": 0}):
+    base_v, base_s = _run(eg, j, queue=1, sorted=1, gcap=45, screen=1)
+    for cfg in ({"queue": 0, "sorted": 1}, {"queue": 0, "sorted": 0}, {"queue": 1, "sorted": 0},
+                {"queue": 1, "sorted": 1, "screen": 0}, {"queue": 1, "sorted": 0, "screen": 1}):
         v, s = _run(eg, j, gcap=45, **cfg)
         assert np.array_equal(s, base_s), cfg
         assert np.array_equal(v, base_v), cfg
-    j.config(queue=1, sorted=1, gcap=45)
+    j.config(queue=1, sorted=1, gcap=45, screen=1)
     j.use_graph(False)
     v, s = _run(eg, j)
     assert np.array_equal(v, base_v) and np.array_equal(s, base_s)
@@ -69,7 +70,7 @@ def test_autotuner_picks_a_measured_candidate(eg, system):
     assert len(trials) >= 4
     assert all(t["msUnit"] > 0 for t in trials)
     best = min(trials, key=lambda t: t["msUnit"])
-    key = ("queue", "sorted", "gcap", "balance")
+    key = ("queue", "sorted", "gcap", "balance", "screen")
     assert tuple(chosen[k] for k in key) == tuple(best[k] for k in key)
     cur = j.config()
     assert tuple(cur[k] for k in key) == tuple(chosen[k] for k in key)
@@ -90,5 +91,18 @@ def test_tuner_rejects_the_plain_path(eg, system):
 
 def test_launches_per_run(eg, system):
     j = eg.Job(system, mode=eg.ECPGB_FAST)
+    j.config(queue=1, screen=1)
+    assert j.launches_per_run() == 10  # reset, 4 per-job stages, 3 screening, unit, scatter
+    j.config(queue=0)
     assert j.launches_per_run() == 7
+    j.close()
+
+
+def test_screening_stage_marks_the_same_units(eg, system):
+    jp = eg.Job(system, mode=eg.ECPGB_FP64)
+    _, ref_s = _run(eg, jp)
+    jp.close()
+    j = eg.Job(system, mode=eg.ECPGB_FAST)
+    _, s = _run(eg, j, queue=1, screen=1)
+    assert np.array_equal(s, ref_s) and (s == 1).any() and (s != 1).any()
     j.close()
