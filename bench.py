@@ -106,12 +106,28 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_sample_system(system):
-    """Bounded CPU sample: 16 of the 50 centres, basis atoms 0..10 (33 shells)."""
-    from libecp_gb300 import workloads as W  # noqa: F401
-    centres = [a for a in range(system.n_atoms) if system.shellsECP[a] > 0][:16]
-    return system.subset(centres=centres, basis_atoms=range(11)), \
-        "16 of 50 centres x 561 pairs (basis atoms 0-10) of the same cluster"
+# the workloads: name -> (description, builder)
+WORKLOADS = {
+    "cluster": WORKLOAD,
+    "cluster8": WORKLOAD + " [first 8 centres]",
+    "mixed_batch": "mixed_batch: 200 shells (20,100 pairs, l<=4, K 1-10, exponents 0.02-200) x 10 ECP centres, FP64",
+    "sweep": "large_sweep: 447 shells (99,681 pairs, l<=4, K 1-6, exponents 0.01-500) x 4 ECP centres "
+             "(L<=5, 6 terms), tolerance 1e-12, FP64",
+}
+
+
+def cpu_sample_system(system, workload="cluster"):
+    """Bounded CPU sample of the workload (the port's time per unit is
+    extrapolated to the whole job)."""
+    centres = [a for a in range(system.n_atoms) if system.shellsECP[a] > 0]
+    if workload in ("cluster", "cluster8"):
+        return system.subset(centres=centres[:16], basis_atoms=range(11)), \
+            "16 of 50 centres x 561 pairs (basis atoms 0-10) of the same cluster"
+    if workload == "mixed_batch":
+        return system.subset(centres=centres[:2], basis_atoms=range(12)), \
+            "2 of 10 centres x the shells of atoms 0-11 of the same batch"
+    return system.subset(centres=centres[:1], basis_atoms=range(12)), \
+        "1 of 4 centres x the shells of atoms 0-11 of the same sweep"
 
 
 _REF_CHILD = """
@@ -120,7 +136,7 @@ sys.path.insert(0, {root!r})
 from oracle import oracle as O
 import bench
 from libecp_gb300 import workloads as W
-sample, _ = bench.cpu_sample_system(bench.make_workload({workload!r}, {seed}))
+sample, _ = bench.cpu_sample_system(bench.make_workload({workload!r}, {seed}), {workload!r})
 cs = [a for a in range(sample.n_atoms) if sample.shellsECP[a] > 0]
 parts = [sample.subset(centres=cs[i::{threads}]) for i in range({threads})]
 t0 = time.perf_counter()
@@ -141,7 +157,7 @@ def run_cpu_baseline(system, threads, workload="cluster", seed=0):
     reported only if it completes.  Returns (units/s, kind, stats, text, units, s).
     """
     from oracle import oracle as O
-    sample, text = cpu_sample_system(system)
+    sample, text = cpu_sample_system(system, workload)
     t0 = time.perf_counter()
     rc, I, st = O.oracle_matrix(sample, nthreads=threads, with_stats=True)
     t_port = time.perf_counter() - t0
@@ -160,6 +176,10 @@ def run_cpu_baseline(system, threads, workload="cluster", seed=0):
 
 def make_workload(name, seed):
     from libecp_gb300 import workloads as W
+    if name == "mixed_batch":
+        return W.mixed_batch(seed)
+    if name == "sweep":
+        return W.large_sweep(seed)
     s = W.batched_cluster(seed=seed)
     if name == "cluster8":
         s = s.subset(centres=[a for a in range(s.n_atoms) if s.shellsECP[a] > 0][:8])
@@ -237,6 +257,21 @@ def ours(args, rank, world):
     if rank == 0 and args.serve_seconds > 0 and mode == eg.ECPGB_FAST:
         serving = serving_run(eg, args.serve_rate, args.serve_seconds)
 
+    mixed = None
+    if rank == 0 and args.mixed_report:
+        # the mixed-precision mode on the same job: speed and error per L class
+        from libecp_gb300.precision import class_errors
+        mj = eg.Job(system, mode=eg.ECPGB_MIXED)
+        mj.tune()
+        mj.run(1, flush_l2=True)
+        mms, _ = mj.run(2, flush_l2=True)
+        mj.close()
+        rep = class_errors(system, eg.raw_blocks(system, eg.ECPGB_FP64), eg.raw_blocks(system, eg.ECPGB_MIXED))
+        mixed = {"value": total_units / (float(np.mean(mms)) / 1e3), "unit": UNIT,
+                 "vs_batched_fp64": (total_units / (float(np.mean(mms)) / 1e3)) / value,
+                 "statuses_equal_fp64": rep["statuses_equal"],
+                 "error_vs_fp64_per_l_class": rep["classes"]}
+
     line = None
     if rank == 0:
         cores = os.cpu_count() or 1
@@ -263,7 +298,7 @@ def ours(args, rank, world):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD if args.workload == "cluster" else WORKLOAD + " [first 8 centres]",
+            "config": {"workload": WORKLOADS[args.workload],
                        "units_per_rank": int(n_units),
                        "emitted_units_per_rank": int(emitted),
                        "path": "batched FP64 (ECPGB_FAST)" if mode != eg.ECPGB_FP64 else "plain FP64 drop-in (ECPGB_FP64)",
@@ -289,6 +324,7 @@ def ours(args, rank, world):
                              "sample": f"{text}: {s_units} units in {s_time:.1f} s"},
             "clocks": clk.summary(),
             "serving": serving,
+            "mixed_precision": mixed,
             "gpu_launches": launches,
             "peaks_measured": peaks,
         }
@@ -353,8 +389,11 @@ def main():
                     help="serving stream arrival rate (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=20.0,
                     help="serving stream length (0: no serving run)")
-    ap.add_argument("--workload", default="cluster", choices=["cluster", "cluster8"],
-                    help="cluster8: the first 8 centres only (small case for profiler captures)")
+    ap.add_argument("--workload", default="cluster", choices=list(WORKLOADS),
+                    help="cluster (the headline), cluster8 (its first 8 centres: profiler captures), "
+                         "mixed_batch and sweep (the other configurations)")
+    ap.add_argument("--mixed-report", type=int, default=0,
+                    help="also run the mixed-precision mode and report its error per L class")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
