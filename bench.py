@@ -319,7 +319,14 @@ def ours(args, rank, world):
                          # F_alg counts the reference's full large-grid tabulation of every
                          # fallback; the batched kernel stops at the converged level, so the
                          # executed work is the ncu FP64 pipe utilisation below
-                         "fp64_pipe_active_ncu": pipe},
+                         "fp64_pipe_active_ncu": pipe,
+                         "note": ("F_alg is the reference's work (its control flow counted by the oracle), "
+                                  "including the full 1023-point large-grid tabulation of every fallback; "
+                                  "the batched kernel tabulates only the levels up to convergence and only "
+                                  "the points whose values are not negligible, with the same quadrature "
+                                  "results, so frac can exceed 1; the executed FP64 work is "
+                                  "fp64_pipe_active_ncu" if kernel != "k_unit" else
+                                  "F_alg is the reference's work, counted by the oracle on its control flow")},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": min(cores, 16), "kind": kind,
                              "sample": f"{text}: {s_units} units in {s_time:.1f} s"},
             "clocks": clk.summary(),
