@@ -68,6 +68,10 @@ struct DevJob {
   const double *besT, *besC;
   const double *besH;          // Taylor coefficients [i][l <= besHL][6] (batched path)
   const double *besA;          // large-argument polynomial [l][i], stride max(besHL + 1, 6)
+  // the level schedules' slot tables in global memory as well, for reads
+  // whose index differs across a warp (the __constant__ copies serialise those)
+  const int *s93, *s92;
+  const short *byN93;          // small-grid slots step by step in ascending point order
   const float *besHf;          // besH in FP32 (mixed mode)
   int besHL;
   const double *shNorm;        // spherical-harmonic normalisation [l][m], side tmDim + 1

@@ -17,8 +17,6 @@
 //     depends on (i, j) only through the index of a_i + b_j
 //     (src/type1.c:323-345), so one accumulator per combined index receives
 //     exactly the terms the reference adds to each chi[i][j].
-#include <algorithm>
-
 #include "ecp_device.cuh"
 #include "ecp_fastmath.h"
 
@@ -29,10 +27,7 @@ constexpr int kWalkCap = 128;  // large-grid quadratures per warp and pass
 constexpr int kLargeWords = (kMaxLargeOrder + 1) / 32;  // bitmap words over the large grid (128, even)
 static_assert(kLargeWords * 32 >= kMaxLargeOrder && kLargeWords % 2 == 0, "large-grid bitmap size");
 
-// The small-grid schedule's slots step by step (33, then 32 at a time) in
-// ascending order of their grid point: a unit's window [ws, we) is then one
-// run of each step, so its points can be dealt to consecutive lanes.
-static __constant__ short c93_byN[kSmallOrder];
+
 // Mixed mode: FP32 integrands carry noise of a few 1e-8 relative, below which
 // no error estimate can fall, so a quadrature also stops once its estimated
 // error is below kMixedRel of its value -- from kMixedMinPoints points on
@@ -403,14 +398,14 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     const int ns = s1 - s0;
     int lo, hi;
     {
-      const int n0 = lane < ns ? c93_slot[c93_byN[s0 + lane]] : INT_MAX;
-      const int n1 = lane + 32 < ns ? c93_slot[c93_byN[s0 + lane + 32]] : INT_MAX;
+      const int n0 = lane < ns ? __ldg(J.s93 + __ldg(J.byN93 + s0 + lane)) : INT_MAX;
+      const int n1 = lane + 32 < ns ? __ldg(J.s93 + __ldg(J.byN93 + s0 + lane + 32)) : INT_MAX;
       lo = __popc(__ballot_sync(0xffffffffu, n0 < ws)) + __popc(__ballot_sync(0xffffffffu, n1 < ws));
       hi = __popc(__ballot_sync(0xffffffffu, n0 < we)) + __popc(__ballot_sync(0xffffffffu, n1 < we));
     }
     const int nIn = hi - lo;
     for (int e = lane; e < nIn * G; e += 32) {
-      const int gg = e % G, t = c93_byN[s0 + lo + e / G], n = c93_slot[t];
+      const int gg = e % G, t = __ldg(J.byN93 + s0 + lo + e / G), n = __ldg(J.s93 + t);
       double *ent = tab + ((t - s0) * G + gg) * TSs;
       const double s = sc[gg * 6];
       double r = J.xSmall[n], ex = (sc[gg * 6 + 4] * r + s) * r;
@@ -424,7 +419,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       }
     }
     for (int e = lane; e < (ns - nIn) * G; e += 32) {
-      const int i = e / G, t = c93_byN[s0 + (i < lo ? i : i + nIn)];
+      const int i = e / G, t = __ldg(J.byN93 + s0 + (i < lo ? i : i + nIn));
       double *ent = tab + ((t - s0) * G + e % G) * TSs;
       for (int l = 0; l < 2 * lq; l++) ent[l] = 0.0;
     }
@@ -497,7 +492,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     for (int s0 = 0; s0 < OL;) {
       const int s1 = step_end92(s0) < OL ? step_end92(s0) : OL;
       for (int t = s0 + lane; t < s1; t += 32) {
-        int n = c92_slot[t];
+        int n = __ldg(J.s92 + t);
         bool upper = t > 0 && ((t - 1) & 1);
         double *e = tab + (t - s0) * TSf;
         double *K = e + 2, *R = e + 2 + lq;
@@ -605,7 +600,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
   // below its break; beyond it, on the lower half, the last earlier pair
   // whose loop reached that point; and the point, exponent of that pair.
   auto locate = [&](int t, int &owner, double &r, double &ex) {
-    const int n = c92_slot[t];
+    const int n = __ldg(J.s92 + t);
     const bool upper = t > 0 && ((t - 1) & 1);
     owner = -1;
     if (n < nb) owner = k;
@@ -658,7 +653,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       while (nE > 0 && pend[nE - 1] >= b) nE--;
     }
     if (lane < nE) {
-      const int t = pend[lane], n = c92_slot[t];
+      const int t = pend[lane], n = __ldg(J.s92 + t);
       int owner;
       double r, ex;
       locate(t, owner, r, ex);
@@ -1081,16 +1076,6 @@ int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, con
                           const int *s92lvEnd, const int *s92lvN, int s92levels, void *stream) {
   if (s93n > kSmallOrder || s92n > kMaxLargeOrder || s93levels > 32 || s92levels > 32) return 1;
   cudaStream_t st = (cudaStream_t)stream;
-  // each step's slots by ascending grid point (the steps of t1_group_run)
-  static short byN[kSmallOrder];
-  for (int s0 = 0; s0 < s93n;) {
-    int s1 = s0 == 0 ? 33 : s0 + 32;
-    if (s1 > s93n) s1 = s93n;
-    for (int t = s0; t < s1; t++) byN[t] = (short)t;
-    std::sort(byN + s0, byN + s1, [&](short a, short b) { return s93slot[a] < s93slot[b]; });
-    s0 = s1;
-  }
-  cudaMemcpyToSymbolAsync(c93_byN, byN, sizeof(short) * s93n, 0, cudaMemcpyHostToDevice, st);
   cudaMemcpyToSymbolAsync(c93_slot, s93slot, sizeof(int) * s93n, 0, cudaMemcpyHostToDevice, st);
   cudaMemcpyToSymbolAsync(c93_lvEnd, s93lvEnd, sizeof(int) * s93levels, 0, cudaMemcpyHostToDevice, st);
   cudaMemcpyToSymbolAsync(c93_lvJ, s93lvJ, sizeof(int) * s93levels, 0, cudaMemcpyHostToDevice, st);

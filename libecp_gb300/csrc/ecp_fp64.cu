@@ -307,7 +307,8 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
         int s1 = s0 == 0 ? 1 + 2 * kChunkPairs : s0 + 2 * kChunkPairs;
         if (s1 > nSlots) s1 = nSlots;
         for (int pos = s0 + tid; pos < s1; pos += NT) {
-          int n = c92_slot[pos];
+          // index differs across the warp: the global copy (constant reads serialise)
+          int n = J.s92 ? __ldg(J.s92 + pos) : c92_slot[pos];
           double *e = ck + (pos - s0) * CS;  // w, ex, vis, U, R[nA], K[nA]
           double *eR = e + 4, *eK = e + 4 + nA;
           bool upper = (pos > 0) && ((pos - 1) & 1);
@@ -543,7 +544,7 @@ __global__ void __launch_bounds__(kUnitThreads, 1) k_unit(DevJob J) {
           int s1 = s0 == 0 ? 1 + 2 * kChunkPairs : s0 + 2 * kChunkPairs;
           if (s1 > OL) s1 = OL;
           for (int pos = s0 + tid; pos < s1; pos += NT) {
-            int n = c92_slot[pos];
+            int n = J.s92 ? __ldg(J.s92 + pos) : c92_slot[pos];
             double *e = ck + (pos - s0) * CS;  // w, ex, vis, U[LE], R[nA], Ka[LBE], Kb[LBE]
             double *eU = e + 3, *eR = eU + LE, *eKa = eR + nA, *eKb = eKa + LBE;
             bool upper = (pos > 0) && ((pos - 1) & 1);

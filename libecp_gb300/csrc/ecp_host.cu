@@ -214,9 +214,25 @@ struct DevTables {
   HostTables host;
   DBuf<float> besHf;
   DBuf<double> xs, ws, xl, wl, besT, besC, besH, besA, shNorm, p2s, fac, dfac, omega, c2s;
-  DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items;
+  DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items, s93, s92;
+  DBuf<short> byN93;
   int nItemsMax = 0;
 };
+
+// The small-grid schedule's slots step by step (33, then 32 at a time) in
+// ascending order of their grid point (the batched kernel's type-1 steps).
+static std::vector<short> by_point_order(const std::vector<int> &slot) {
+  const int n = (int)slot.size();
+  std::vector<short> out(n);
+  for (int s0 = 0; s0 < n;) {
+    int s1 = s0 == 0 ? 33 : s0 + 32;
+    if (s1 > n) s1 = n;
+    for (int t = s0; t < s1; t++) out[t] = (short)t;
+    std::sort(out.begin() + s0, out.begin() + s1, [&](short a, short b) { return slot[a] < slot[b]; });
+    s0 = s1;
+  }
+  return out;
+}
 
 // Two table sets share level schedules when their grids are the same.
 static bool same_schedules(const DevTables *a, const DevTables *b) {
@@ -273,7 +289,8 @@ struct Engine {
               t->fac.upload(h.fac, stream) && t->dfac.upload(h.dfac, stream) &&
               t->omega.upload(h.omega, stream) && t->ijk.upload(h.ijk, stream) &&
               t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) && t->besA.upload(h.besselA, stream) && t->besHf.upload(h.besselHf, stream) &&
-              t->c2s.upload(h.cart2sph, stream) &&
+              t->c2s.upload(h.cart2sph, stream) && t->s93.upload(h.s93.slot, stream) &&
+              t->s92.upload(h.s92.slot, stream) && t->byN93.upload(by_point_order(h.s93.slot), stream) &&
               t->shNorm.upload(h.shNorm, stream);
     // used-triple lists per (la, lb, l)
     int LB = h.maxLBS, LE = h.maxLECP > 0 ? h.maxLECP : 1;
@@ -524,6 +541,9 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.besH = T->besH.p;
   J.besA = T->besA.p;
   J.besHf = T->besHf.p;
+  J.s93 = T->s93.p;
+  J.s92 = T->s92.p;
+  J.byN93 = T->byN93.p;
   J.mixed = mode == ECPGB_MIXED;
   J.besHL = h.besselHL;
   J.shNorm = T->shNorm.p;
