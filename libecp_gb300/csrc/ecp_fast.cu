@@ -404,8 +404,23 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       hi = __popc(__ballot_sync(0xffffffffu, n0 < we)) + __popc(__ballot_sync(0xffffffffu, n1 < we));
     }
     const int nIn = hi - lo;
-    for (int e = lane; e < nIn * G; e += 32) {
-      const int gg = e % G, t = __ldg(J.byN93 + s0 + lo + e / G), n = __ldg(J.s93 + t);
+    // only the pairs of the group with a quadrature still running are
+    // tabulated: a converged lane reads no entry again
+    unsigned live = 0;
+    {
+      const unsigned run = __ballot_sync(0xffffffffu, !done), qm = nq >= 32 ? ~0u : (1u << nq) - 1u;
+      for (int gg = 0; gg < G; gg++)
+        if (run >> (gg * nq) & qm) live |= 1u << gg;
+    }
+    const int nLive = __popc(live);
+    // the i-th live pair of the group
+    auto live_pair = [&](int i) {
+      unsigned m = live;
+      for (; i > 0; i--) m &= m - 1u;
+      return __ffs(m) - 1;
+    };
+    for (int e = lane; e < nIn * nLive; e += 32) {
+      const int gg = live_pair(e % nLive), t = __ldg(J.byN93 + s0 + lo + e / nLive), n = __ldg(J.s93 + t);
       double *ent = tab + ((t - s0) * G + gg) * TSs;
       const double s = sc[gg * 6];
       double r = J.xSmall[n], ex = (sc[gg * 6 + 4] * r + s) * r;
@@ -418,9 +433,9 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
         rl = r * rl;
       }
     }
-    for (int e = lane; e < (ns - nIn) * G; e += 32) {
-      const int i = e / G, t = __ldg(J.byN93 + s0 + (i < lo ? i : i + nIn));
-      double *ent = tab + ((t - s0) * G + e % G) * TSs;
+    for (int e = lane; e < (ns - nIn) * nLive; e += 32) {
+      const int i = e / nLive, t = __ldg(J.byN93 + s0 + (i < lo ? i : i + nIn));
+      double *ent = tab + ((t - s0) * G + live_pair(e % nLive)) * TSs;
       for (int l = 0; l < 2 * lq; l++) ent[l] = 0.0;
     }
     __syncwarp();
@@ -624,6 +639,10 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
   // queued.
   unsigned doneBits[kWalkCap / 32] = {0u, 0u, 0u, 0u};
   int cpos = 0, wpos = 0, nPend = 0;
+  // channels and rows the quadratures still running read (the pass's to
+  // begin with, narrowed after every walk)
+  unsigned pMask = S.passMask;
+  int pL1 = S.passL1, pL2 = S.passL2, pL3 = S.passL3;
   const unsigned below = (1u << lane) - 1u;
   while (wpos < OL) {
     while (nPend < 32 && cpos < OL) {
@@ -663,12 +682,12 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       // Ka rows carry the weight and prefactor: w * Ck * e^(..) * K_l1
       const double wB = (J.wLarge[n] * i1) * (Ck * fast_exp(ex));
       // only the channels and rows this pass's quadratures read
-      channels_masked(J, c, r, S.passMask, U);
-      bessel_fast(J, S.passL1, 2.0 * zaj * dAC * r, Ka, 1);
-      for (int l = 0; l <= S.passL1; l++) Ka[l] *= wB;
-      bessel_fast(J, S.passL2, 2.0 * zbj * dBC * r, Kb, 1);
+      channels_masked(J, c, r, pMask, U);
+      bessel_fast(J, pL1, 2.0 * zaj * dAC * r, Ka, 1);
+      for (int l = 0; l <= pL1; l++) Ka[l] *= wB;
+      bessel_fast(J, pL2, 2.0 * zbj * dBC * r, Kb, 1);
       R[0] = 1.0;
-      for (int l = 1; l <= S.passL3; l++) R[l] = r * R[l - 1];
+      for (int l = 1; l <= pL3; l++) R[l] = r * R[l - 1];
     }
     if (lane == 0) {  // entry of slot t: queued slots in [wpos, t)
       const int w0 = wpos >> 5, w1 = (b - 1) >> 5;
@@ -680,6 +699,8 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
     }
     __syncwarp();
     bool all = true;
+    unsigned nMask = 0u;
+    int n1 = 0, n2 = 0, n3 = 0;
     for (int q = lane, qi = 0; q < nf; q += 32, qi++) {
       if (doneBits[qi] & (1u << lane)) continue;
       int v = S.failIdx[q], l = 0, qq = v;
@@ -699,8 +720,18 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       psm92_advance(wpos, b, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
       sI[q] = I; sP[q] = p; sQ[q] = qv;
       if (done) { sR[q] = res; doneBits[qi] |= 1u << lane; }
-      else all = false;
+      else {
+        all = false;
+        nMask |= 1u << l;
+        n1 = l1 > n1 ? l1 : n1;
+        n2 = l2 > n2 ? l2 : n2;
+        n3 = l3 > n3 ? l3 : n3;
+      }
     }
+    pMask = __reduce_or_sync(0xffffffffu, nMask);
+    pL1 = __reduce_max_sync(0xffffffffu, n1);
+    pL2 = __reduce_max_sync(0xffffffffu, n2);
+    pL3 = __reduce_max_sync(0xffffffffu, n3);
     // drop the evaluated slots from the queue
     const int rest = nPend - nE;
     const int keep0 = lane < rest ? pend[nE + lane] : 0, keep1 = lane + 32 < rest ? pend[nE + lane + 32] : 0;
