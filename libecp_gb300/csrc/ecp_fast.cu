@@ -83,11 +83,18 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
   }
   for (int l = 0; l <= lmax; l++) {
     const double *q = cf + l * cs;
-    double v = 0.0;
-    for (int k = l; k > 5; k--) v = fma(v, x, asy ? q[k] : 0.0);
+    // Horner from the row's top coefficient (degree l on the large-argument
+    // branch above 5, else 5): no multiply of a zero, no scaling by 1
+    int k = asy && l > 5 ? l : 5;
+    double v = q[k];
+    while (k > 5) {
+      k--;
+      v = fma(v, x, q[k]);
+    }
 #pragma unroll
-    for (int k = 5; k >= 0; k--) v = fma(v, x, q[k]);
-    K[l * stride] = v * mult;
+    for (int j = 4; j >= 0; j--) v = fma(v, x, q[j]);
+    if (asy) v *= mult;
+    K[l * stride] = v;
   }
 }
 
@@ -427,10 +434,11 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
       const double wB = J.wSmall[n] * (sc[gg * 6 + 3] * uL[n] * ex);
       bessel_fast(J, lab, s * r, ent, 1);
-      double *WR = ent + lq, rl = 1.0;
-      for (int l = 0; l <= lab; l++) {
-        WR[l] = wB * rl;
-        rl = r * rl;
+      double *WR = ent + lq, v = wB;
+      WR[0] = v;
+      for (int l = 1; l <= lab; l++) {
+        v *= r;
+        WR[l] = v;
       }
     }
     for (int e = lane; e < (ns - nIn) * nLive; e += 32) {
@@ -506,20 +514,27 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     bool done2 = !fail;
     for (int s0 = 0; s0 < OL;) {
       const int s1 = step_end92(s0) < OL ? step_end92(s0) : OL;
+      // the rows the quadratures still running read
+      const int kq = __reduce_max_sync(0xffffffffu, done2 ? 0 : l2);
+      const int rq = __reduce_max_sync(0xffffffffu, done2 ? 0 : l1);
       for (int t = s0 + lane; t < s1; t += 32) {
         int n = __ldg(J.s92 + t);
         bool upper = t > 0 && ((t - 1) & 1);
-        double *e = tab + (t - s0) * TSf;
-        double *K = e + 2, *R = e + 2 + lq;
-        e[0] = J.wLarge[n] * i1;
-        e[1] = 0.0;
-        if (n < nb) {
+        // entry: K_l rows, then the rows w * C2 U_L e^(..) r^l
+        double *K = tab + (t - s0) * TSf, *WR = K + lq;
+        const double w = J.wLarge[n] * i1;
+        bool any = false;
+        if (n < nb && !(upper && n > end)) {
           double r = i1 * J.xLarge[n] + i2, ex = (z * r + s) * r + zd2;
           if (ex >= J.lnAcc1) {
-            e[1] = C2 * channel(J, c, Lc, r) * fast_exp(ex);
-            bessel_fast(J, lab, s * r, K, 1);
-            R[0] = 1.0;
-            for (int l = 1; l <= lab; l++) R[l] = r * R[l - 1];
+            double v = w * (C2 * channel(J, c, Lc, r) * fast_exp(ex));
+            any = v != 0.0;
+            bessel_fast(J, kq, s * r, K, 1);
+            WR[0] = v;
+            for (int l = 1; l <= rq; l++) {
+              v *= r;
+              WR[l] = v;
+            }
           }
         } else if (n != nb && !upper && n < O && n >= ws && n < we) {
           // beyond the break the reference integrates its small-grid buffers:
@@ -527,24 +542,28 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
           // rows written with the small grid's stride
           double rs = J.xSmall[n], es = (z * rs + s) * rs;
           if (es >= J.lnAcc1) {
-            e[1] = C2 * uL[n] * fast_exp(es);
+            const double v = w * (C2 * uL[n] * fast_exp(es));
+            any = v != 0.0;
             for (int l = 0; l <= lab; l++) {
               int f = l * OL + n, lr = f / O, nr = f % O;
               bool ok = lr <= lab && nr >= ws && nr < we;
               double xr = J.xSmall[nr], pw = 1.0;
               for (int i = 0; i < lr && ok; i++) pw = xr * pw;
-              R[l] = ok ? pw : 0.0;
+              WR[l] = ok ? v * pw : 0.0;
               K[l] = ok ? bessel_row(J, lr, s * xr) : 0.0;
             }
           }
         }
-        if (upper && n > end) e[1] = 0.0;
+        if (!any) {
+          for (int l = 0; l <= kq; l++) K[l] = 0.0;
+          for (int l = 0; l <= rq; l++) WR[l] = 0.0;
+        }
       }
       __syncwarp();
       if (!done2) {
         auto val = [&](int t) {
           const double *e = tab + (t - s0) * TSf;
-          return e[1] == 0.0 ? 0.0 : e[0] * (e[1] * e[2 + lq + l1] * e[2 + l2]);
+          return e[lq + l1] * e[l2];
         };
         auto vis = [&](int t) { return c92_slot[t] <= end; };
         psm92_advance(s0, s1, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I2, p2, q2, done2, res2);
