@@ -94,6 +94,7 @@ struct DevJob {
   const int *order;              // units by descending estimated cost (null: natural order)
   unsigned long long *queueHead; // next queue position (persistent launch); reset per run
   int gcap;                      // type-1 step-table width cap (doubles per slot per warp)
+  int maxNP;                     // most primitive pairs of a shell pair (shared-memory sizing)
   int mixed;                     // 1: FP32 Bessel Taylor rows and ECP channel terms
   int balance;                   // 1: type-1 groups narrowed so that every warp gets pairs
   // screening stage (batched path): the queue of units that compute blocks
@@ -198,7 +199,7 @@ void launch_epilogue(const DevJob &job, cudaStream_t stream);
 int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, const int *s93lvJ,
                           const int *s93lvN, int s93levels, const int *s92slot, int s92n,
                           const int *s92lvEnd, const int *s92lvN, int s92levels, void *stream);
-size_t fast_smem_bytes(int LB, int LE, int nF, int gcap);
+size_t fast_smem_bytes(int LB, int LE, int nF, int gcap, int maxNP);
 // CTAs of the batched unit kernel resident per SM at smemBytes.
 int fast_ctas_per_sm(size_t smemBytes, int queue);
 // Sets the batched kernels' function attributes on the current device (call

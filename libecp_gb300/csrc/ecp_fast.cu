@@ -239,9 +239,10 @@ struct FastSmem {
   // type-2 fallback per warp (inside phase)
   int w2Stride, w2Tab, w2I, w2P, w2Q, w2R, w2Part, tab2Stride;
   int w2Bits, w2Pend, w2Pref;  // fallback streaming: needed-slot bitmap, pending slots, word prefixes
+  int ppMap;                   // type-2 fallback: FM06 map (i1, i2) of every primitive pair
 };
 
-__host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap) {
+__host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap, int maxNP) {
   FastSmem s{};
   const int nA = 2 * LB + 1, nE = LE > 0 ? LE : 1, LBE = LB + nE;
   const int nc = (LB + 1) * (LB + 2) * (LB + 3) / 6, nct = (LB + 1) * (LB + 2) / 2;
@@ -282,7 +283,8 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap)
   s.w2Pend = s.w2Bits + kLargeWords / 2;      // 64 int
   s.w2Pref = s.w2Pend + 32;                   // kLargeWords int
   s.w2Stride = s.w2Pref + kLargeWords / 2;
-  int t2b = kWarps * s.w2Stride;
+  s.ppMap = kWarps * s.w2Stride;
+  int t2b = s.ppMap + 2 * maxNP;
   int ph = t1;
   if (t2a > ph) ph = t2a;
   if (t2b > ph) ph = t2b;
@@ -290,8 +292,8 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap)
   return s;
 }
 
-size_t fast_smem_bytes(int LB, int LE, int nF, int cap) {
-  return sizeof(double) * (size_t)fast_layout(LB, LE, nF, cap).total;
+size_t fast_smem_bytes(int LB, int LE, int nF, int cap, int maxNP) {
+  return sizeof(double) * (size_t)fast_layout(LB, LE, nF, cap, maxNP).total;
 }
 
 struct FastShared {
@@ -498,16 +500,31 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     const double C2 = ca * cb;
     double i1, i2;
     fm06(za, zb, dAC, dBC, i1, i2);
-    int nb = OL;  // first point past both centres whose exponent is below the screen
-    for (int n0 = 0; n0 < OL; n0 += 32) {
-      int n = n0 + lane;
-      bool pr = false;
-      if (n < OL) {
-        double r = i1 * J.xLarge[n] + i2, e = (z * r + s) * r + zd2;
-        pr = r > dAC && r > dBC && e < J.lnAcc1;
+    // first point past both centres whose exponent is below the screen
+    // (src/type1.c:168-176).  Past both centres the exponent falls as r
+    // grows, so the predicate is monotone in the index: a 32-way search,
+    // first over the last points of 32 chunks, then inside the first chunk
+    // whose last point qualifies.
+    auto brk = [&](int n) {
+      const double r = i1 * J.xLarge[n] + i2, e = (z * r + s) * r + zd2;
+      return r > dAC && r > dBC && e < J.lnAcc1;
+    };
+    const int chunk = (OL + 31) / 32;
+    int nb = OL;
+    {
+      const int n = lane * chunk + chunk - 1 < OL ? lane * chunk + chunk - 1 : OL - 1;
+      const unsigned b = __ballot_sync(0xffffffffu, brk(n));
+      if (b) {
+        const int n0 = (__ffs(b) - 1) * chunk;
+        for (int c0 = n0; c0 < n0 + chunk && c0 < OL; c0 += 32) {
+          const int m = c0 + lane;
+          const unsigned b2 = __ballot_sync(0xffffffffu, m < n0 + chunk && m < OL && brk(m));
+          if (b2) {
+            nb = c0 + __ffs(b2) - 1;
+            break;
+          }
+        }
       }
-      unsigned b = __ballot_sync(0xffffffffu, pr);
-      if (b) { nb = n0 + __ffs(b) - 1; break; }
     }
     const int end = nb - 1;
     double I2 = 0, p2 = 0, q2 = 0, res2 = 0;
@@ -612,7 +629,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
 static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, const FastShared &S,
                                int k, int Nb, int nf, int c, int Lc, int la, int lb, const double *pzA,
                                const double *pcA, const double *pzB, const double *pcB, double dAC,
-                               double dBC, int ncls, int pa0, int pb0, int &warn) {
+                               double dBC, int ncls, int pa0, int pb0, const double *map, int &warn) {
   const int lane = threadIdx.x & 31, nA = 2 * J.maxLBS + 1;
   const int LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE, OL = J.largeOrder;
   const int TS = L.tab2Stride;
@@ -624,8 +641,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
   // derivative blocks: the product times zeta_a^max(0, shifta), then
   // zeta_b^max(0, shiftb) (src/type2.c:456-462)
   const double Ck = zeta_times(zeta_times(ca * cb, za, pa0), zb, pb0);
-  double i1, i2;
-  fm06(za, zb, dAC, dBC, i1, i2);
+  const double i1 = map[2 * k];
   const int nb = S.ppBreak[k], end = nb == INT_MAX ? OL - 1 : nb - 1;
   for (int q = lane; q < nf; q += 32) { sI[q] = 0; sP[q] = 0; sQ[q] = 0; sR[q] = 0; }
   for (int w = lane; w < (OL + 31) / 32; w += 32) needBits[w] = 0u;
@@ -645,9 +661,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
     }
     if (owner < 0) return;
     const double zaj = pzA[owner / Nb], zbj = pzB[owner % Nb];
-    double i1j = i1, i2j = i2;
-    if (owner != k) fm06(zaj, zbj, dAC, dBC, i1j, i2j);
-    r = i1j * J.xLarge[n] + i2j;
+    r = map[2 * owner] * J.xLarge[n] + map[2 * owner + 1];
     const double d1 = dAC - r, d2 = dBC - r;
     ex = -zaj * d1 * d1 - zbj * d2 * d2;
   };
@@ -793,7 +807,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     if (tid == 0) J.status[u] = kUnitSkipped;
     return;
   }
-  const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.nF, J.gcap);
+  const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.nF, J.gcap, J.maxNP);
   const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa] + sh.a, lb = J.shL[sb] + sh.b, lab = la + lb;
   const int lpa = sh.lpa, lpb = sh.lpb, pa0 = sh.a > 0 ? sh.a : 0, pb0 = sh.b > 0 ? sh.b : 0;
   const int nA = 2 * J.maxLBS + 1, LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE;
@@ -924,9 +938,12 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   if (S.nFail > 0) {
     // break index of every primitive pair (bisection: the break predicate is
     // monotone in the index beyond both centres)
+    double *map = ph + Lm.ppMap;  // (the small-grid stage's F tables are no longer read)
     for (int k = tid; k < NP; k += NT) {
       double za = pzA[k / Nb], zb = pzB[k % Nb], i1, i2;
       fm06(za, zb, dAC, dBC, i1, i2);
+      map[2 * k] = i1;
+      map[2 * k + 1] = i2;
       int lo = 0, hi = J.largeOrder;
       while (lo < hi) {
         int mid = (lo + hi) >> 1;
@@ -966,7 +983,8 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       for (int q = tid & 31; q < nf; q += 32) W[Lm.w2Part + q] = 0.0;
       __syncwarp();
       for (int k = warp; k < NP; k += kWarps)
-        t2_pair(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0, warn2);
+        t2_pair(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0, ph + Lm.ppMap,
+                warn2);
       __syncthreads();
       for (int q = tid; q < nf; q += NT) {
         double v = 0.0;

@@ -460,6 +460,7 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.angC = ncum(h.maxLBS);
   J.uspD = h.maxLBS + 1;
   J.largeOrder = (int)h.xl.size();
+  for (int k : P.shK) J.maxNP = std::max(J.maxNP, k * k);
   J.tol = P.tol; J.acc = P.acc;
   J.lnAcc1 = std::log(P.acc) - 2;
   J.lnAcc2 = std::log(1.0E-14) - 2;
@@ -562,7 +563,7 @@ int run_pipeline(JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0, cudaE
   if (mode == ECPGB_FAST || mode == ECPGB_MIXED) {
     FastConfig c = cfg ? *cfg : engine().config_for(J.maxLBS, J.maxLECP);
     c.mixed = mode == ECPGB_MIXED;
-    rc = launch_fast_pipeline(J, stream, fast_smem_bytes(J.maxLBS, J.maxLECP, J.nF, c.gcap), c, u0, u1);
+    rc = launch_fast_pipeline(J, stream, fast_smem_bytes(J.maxLBS, J.maxLECP, J.nF, c.gcap, J.maxNP), c, u0, u1);
   } else {
     rc = launch_fp64_pipeline(J, stream, B.smem, u0, u1);
   }
@@ -983,7 +984,7 @@ int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials,
   FastConfig bestCfg = R->cfg;
   int n = 0;
   for (const FastConfig &c : cand) {
-    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap), c.queue) < 1) continue;
+    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap, R->J.maxNP), c.queue) < 1) continue;
     float tot = 0;
     for (int r = 0; r < 3; r++) {
       cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
@@ -1027,7 +1028,7 @@ int job_config(void *vj, const ecpgb_launch_config *cfg, ecpgb_launch_config *ou
     c.gcap = cfg->gcap;
     c.balance = cfg->balance ? 1 : 0;
     c.screen = cfg->screen ? 1 : 0;
-    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap), c.queue) < 1) {
+    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap, R->J.maxNP), c.queue) < 1) {
       set_error("configuration does not fit on an SM");
       return 1;
     }
