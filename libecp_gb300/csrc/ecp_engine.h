@@ -73,6 +73,7 @@ struct DevJob {
   const int *s93, *s92;
   const short *byN93;          // small-grid slots step by step in ascending point order
   const float *besHf;          // besH in FP32 (mixed mode)
+  const double *besZ;          // Bessel table abscissae i / (besselN / 16)
   int besHL;
   const double *shNorm;        // spherical-harmonic normalisation [l][m], side tmDim + 1
   const double *p2s, *fac, *dfac;

@@ -62,7 +62,7 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
   } else {
     const double h = J.besselN / 16;  // integer division, as the reference
     const int index = (int)floor(z * h + 0.5);
-    x = z - index / h;
+    x = z - __ldg(J.besZ + index);  // index / h, tabulated
     if (J.mixed) {
       // mixed mode: the Taylor rows in FP32 (every lane of the warp is on
       // this branch or the large-argument one, which stays FP64)
@@ -107,7 +107,7 @@ static __device__ double bessel_row(const DevJob &J, int l, double z) {
   }
   double h = J.besselN / 16;
   int index = (int)floor(z * h + 0.5);
-  double dz = z - index / h;
+  double dz = z - __ldg(J.besZ + index);  // index / h, tabulated
   const double *q = J.besH + ((size_t)index * (J.besHL + 1) + l) * 6;
   double v = fma(q[5], dz, q[4]);
   v = fma(v, dz, q[3]);

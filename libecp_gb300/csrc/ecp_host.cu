@@ -213,7 +213,7 @@ struct DevTables {
   TableKey key{};
   HostTables host;
   DBuf<float> besHf;
-  DBuf<double> xs, ws, xl, wl, besT, besC, besH, besA, shNorm, p2s, fac, dfac, omega, c2s;
+  DBuf<double> xs, ws, xl, wl, besT, besC, besH, besA, besZ, shNorm, p2s, fac, dfac, omega, c2s;
   DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items, s93, s92;
   DBuf<short> byN93;
   int nItemsMax = 0;
@@ -289,6 +289,7 @@ struct Engine {
               t->fac.upload(h.fac, stream) && t->dfac.upload(h.dfac, stream) &&
               t->omega.upload(h.omega, stream) && t->ijk.upload(h.ijk, stream) &&
               t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) && t->besA.upload(h.besselA, stream) && t->besHf.upload(h.besselHf, stream) &&
+              t->besZ.upload(h.besselZ, stream) &&
               t->c2s.upload(h.cart2sph, stream) && t->s93.upload(h.s93.slot, stream) &&
               t->s92.upload(h.s92.slot, stream) && t->byN93.upload(by_point_order(h.s93.slot), stream) &&
               t->shNorm.upload(h.shNorm, stream);
@@ -541,6 +542,7 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.gcap = FastConfig{}.gcap;
   J.besH = T->besH.p;
   J.besA = T->besA.p;
+  J.besZ = T->besZ.p;
   J.besHf = T->besHf.p;
   J.s93 = T->s93.p;
   J.s92 = T->s92.p;

@@ -420,6 +420,9 @@ void bessel_horner(HostTables &t) {
     }
   }
   t.besselHf.assign(t.besselH.begin(), t.besselH.end());
+  const double h = t.besselN / 16;  // integer division, as src/bessel.c:138-143
+  t.besselZ.resize(N);
+  for (int i = 0; i < N; i++) t.besselZ[i] = i / h;
   const int AS = HL + 1 < 6 ? 6 : HL + 1;
   t.besselA.assign((size_t)(HL + 1) * AS, 0.0);
   for (int l = 0; l <= HL; l++) {

@@ -81,6 +81,7 @@ struct HostTables {
   // reference's running product divided by i!, so they are exact in FP64.
   std::vector<double> besselA;
   std::vector<float> besselHf;   // besselH rounded to FP32 (mixed-precision mode)
+  std::vector<double> besselZ;   // table abscissae z_i = i / (besselN / 16), the reference's division
   // Normalisation of the real spherical harmonics, [l][m] for l, m <= tmDim:
   // sqrt((2l+1)/(2 pi)) and sqrt((l-m)!/(l+m)!) times that, computed as
   // src/spherical_harmonics.c:236-243 does.
