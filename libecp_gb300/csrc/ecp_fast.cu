@@ -201,7 +201,7 @@ static __device__ inline void psm92_advance(int s0, int s1, double tol, double r
       double N = c92_lvN[k] + 1.0, e = I - p;
       // mixed mode: the reference's two-difference test with the tolerance
       // raised to rel times the estimate
-      const double t = N >= kMixedMinPoints ? fmax(tol, rel * fabs(16 * I / (3 * N))) : tol;
+      const double t = rel > 0.0 && N >= kMixedMinPoints ? fmax(tol, rel * fabs(16 * I / (3 * N))) : tol;
       if (16 * e * e <= 3 * N * fabs(I - q) * t) {
         res = 16 * I / (3 * N);
         done = true;
@@ -209,6 +209,38 @@ static __device__ inline void psm92_advance(int s0, int s1, double tol, double r
       k++;
     }
   }
+}
+
+// PS93 walk of ps93_walk (src/gc_integrators.c:157-217) with the error test
+// 16 d / (3 n) < tol written as 16 d < tol 3 n: no divide per level (the
+// same decision but within an ulp of the threshold).
+template <class Fn>
+static __device__ bool ps93_walk_fast(const double *w, int start, int end, double tol, Fn f, double &res) {
+  int mid = c93_slot[0], a = c93_slot[1], b = c93_slot[2];
+  double p = w[mid] * f(mid);
+  double q = w[a] * f(a) + w[b] * f(b);
+  double I = p + q;
+  int pos = 3;
+  for (int k = 0; k < c93_nLevels; k++) {
+    int j = c93_lvJ[k], cnt = 0, e = c93_lvEnd[k];
+    for (; pos < e; pos += 2) {
+      int lo = c93_slot[pos], hi = c93_slot[pos + 1];
+      double T = 0.0;
+      if (lo >= start) { T += w[lo] * f(lo); cnt++; }
+      if (hi <= end) { T += w[hi] * f(hi); cnt++; }
+      I += T;
+    }
+    int n = c93_lvN[k];
+    p += (1 - j) * (I - q);
+    const double d = fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q));
+    q = (1 - j) * q + j * I;
+    if (cnt == 0) continue;
+    if (16 * d < tol * (3 * n)) {
+      res = 16 * q / (3 * n);
+      return true;
+    }
+  }
+  return false;
 }
 
 // --------------------------------------------------------------- layout
@@ -308,15 +340,48 @@ struct FastShared {
 
 // --------------------------------------------------------------- type 1
 
+// 1/k, k <= 24 (the Legendre recurrence's divisor l - m)
+static __device__ const double kRecip[25] = {0.0,        1.0,        1.0 / 2,  1.0 / 3,  1.0 / 4,
+                                             1.0 / 5,    1.0 / 6,    1.0 / 7,  1.0 / 8,  1.0 / 9,
+                                             1.0 / 10,   1.0 / 11,   1.0 / 12, 1.0 / 13, 1.0 / 14,
+                                             1.0 / 15,   1.0 / 16,   1.0 / 17, 1.0 / 18, 1.0 / 19,
+                                             1.0 / 20,   1.0 / 21,   1.0 / 22, 1.0 / 23, 1.0 / 24};
+
+// Direction of the k-vector P as (cos theta, cos phi, sin phi), the values
+// src/util.c:75-106 and src/spherical_harmonics.c:16-114 produce through
+// theta = acos(z/r), phi = atan(y/x) (+pi) and their cosines and sines,
+// computed here without the inverse and direct trigonometric functions (the
+// same values within a few ulps; the reference's special cases -- r or x
+// below 1e-14 -- are kept).
+static __device__ void direction(const double *P, double &ct, double &cp, double &sp) {
+  const double eps = 1.0E-14, x = P[0], y = P[1], z = P[2];
+  const double r = sqrt(x * x + y * y + z * z);
+  ct = r < eps ? 1.0 : fmin(1.0, fmax(-1.0, z / r));
+  if (fabs(x) < eps) {
+    if (fabs(y) < eps) {
+      cp = 1.0;
+      sp = 0.0;
+    } else {
+      const double ph = y < 0.0 ? 1.5 * kPi : 0.5 * kPi;
+      cp = cos(ph);
+      sp = sin(ph);
+    }
+  } else {
+    const double t = y / x, h = 1.0 / sqrt(1.0 + t * t);  // cos(atan t), sin = t cos
+    cp = x > 0.0 ? h : -h;
+    sp = x > 0.0 ? t * h : -(t * h);
+  }
+}
+
 // Column m of the real spherical harmonics S_lm, l = m..lmax, into rsh[l*l +
 // l -/+ m]: the associated Legendre recurrence, normalisation and sin/cos(m
-// phi) recurrence of src/spherical_harmonics.c:16-114, one column per lane.
-static __device__ void rsh_column(const DevJob &J, int lmax, int m, double theta, double phi,
+// phi) recurrence of src/spherical_harmonics.c:16-114, one column per lane;
+// x = cos theta, (c1, s1) = (cos phi, sin phi).
+static __device__ void rsh_column(const DevJob &J, int lmax, int m, double x, double c1, double s1,
                                   double *rsh) {
   const int W = J.tmDim + 1;
   double sm = 0.0, cm = 1.0;
-  if (m > 0 && phi != 0.0) {
-    double s1 = sin(phi), c1 = cos(phi);
+  if (m > 0) {
     sm = s1;
     cm = c1;
     for (int i = 2; i <= m; i++) {
@@ -325,23 +390,23 @@ static __device__ void rsh_column(const DevJob &J, int lmax, int m, double theta
       cm = cn;
     }
   }
-  double x = cos(theta), P2 = 0.0, P1 = 0.0, P = 0.0;
+  double P2 = 0.0, P1 = 0.0, P = 0.0;
   double sp = 1.0;
   if (x != 1.0 && x != -1.0) {
-    double s1 = sqrt(1.0 - x * x);
-    sp = s1;
-    for (int i = 2; i <= m; i++) sp = sp * s1;
+    double st = sqrt(1.0 - x * x);
+    sp = st;
+    for (int i = 2; i <= m; i++) sp = sp * st;
   }
   for (int l = m; l <= lmax; l++) {
     if (1.0 == x) P = (m == 0) ? 1.0 : 0.0;
     else if (-1.0 == x) P = (m == 0) ? (l == 0 ? 1.0 : -P1) : 0.0;
     else if (l == m) P = (m == 0) ? 1.0 : sp * J.dfac[2 * m - 1];
     else if (l == m + 1) P = x * (2 * m + 1) * P1;
-    else P = (x * (2 * l - 1) * P1 - (l + m - 1) * P2) / (l - m);
+    else P = (x * (2 * l - 1) * P1 - (l + m - 1) * P2) * __ldg(kRecip + (l - m));
     P2 = P1;
     P1 = P;
     double v = J.shNorm[l * W + m] * P;
-    if (m == 0) rsh[l * l + l] = v / sqrt(2.0);
+    if (m == 0) rsh[l * l + l] = v * 0x1.6a09e667f3bcdp-1;  // v / sqrt(2)
     else {
       rsh[l * l + l - m] = v * sm;
       rsh[l * l + l + m] = v * cm;
@@ -370,12 +435,10 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     // derivative blocks: coefficients times zeta^max(0, shift) (src/type1.c:239-246)
     double za = pzA[k / Nb], ca = zeta_times(pcA[k / Nb], za, pa0), zb = pzB[k % Nb],
            cb = zeta_times(pcB[k % Nb], zb, pb0);
-    double P[3], Sp[3];
+    double P[3];
     for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * gA[i] + zb * gB[i]);
-    to_spherical(P, Sp);
-    sc[lane * 6 + 0] = Sp[0];
-    sc[lane * 6 + 1] = Sp[1];
-    sc[lane * 6 + 2] = Sp[2];
+    sc[lane * 6 + 0] = sqrt(P[0] * P[0] + P[1] * P[1] + P[2] * P[2]);  // |P|, as src/util.c:75-106
+    direction(P, sc[lane * 6 + 1], sc[lane * 6 + 2], sc[lane * 6 + 5]);
     sc[lane * 6 + 3] = ca * cb * fast_exp(-za * dAC * dAC - zb * dBC * dBC);
     sc[lane * 6 + 4] = -za - zb;
   }
@@ -383,7 +446,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
   // (2) S_lm of every pair, one (pair, m) column per lane
   if (lane < G * lq) {
     int g = lane / lq, m = lane % lq;
-    rsh_column(J, lab, m, sc[g * 6 + 1], sc[g * 6 + 2], rsh + g * RQ);
+    rsh_column(J, lab, m, sc[g * 6 + 1], sc[g * 6 + 2], sc[g * 6 + 5], rsh + g * RQ);
   }
   for (int e = lane; e < G * RQ; e += 32) Q[e] = 0.0;
   __syncwarp();
@@ -396,7 +459,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     while (l1 <= lab && rem >= l1 / 2 + 1) { rem -= l1 / 2 + 1; l1++; }
     l2 = l1 - 2 * rem;
   }
-  double I = 0, p = 0, q = 0, err = 0;
+  double I = 0, p = 0, q = 0;
   bool done = !mine;
   int k = 0, cnt = 0;
   for (int s0 = 0; s0 < O;) {
@@ -473,9 +536,12 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
         int j = c93_lvJ[k], n = c93_lvN[k];
         if (!done) {
           p += (1 - j) * (I - q);
-          if (cnt > 0) err = 16 * fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q)) / (3 * n);
+          // the reference's error estimate is 16 d / (3 n); tested as
+          // 16 d < tol 3 n (no divide; the same decision but within an ulp
+          // of the threshold)
+          const double d = fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q));
           q = (1 - j) * q + j * I;
-          if (cnt > 0 && (err < J.tol || (n >= kMixedMinPoints && err < rel * fabs(16 * q / (3 * n))))) {
+          if (cnt > 0 && (16 * d < J.tol * (3 * n) || (rel > 0.0 && n >= kMixedMinPoints && d < rel * fabs(q)))) {
             done = true;
             Q[g * RQ + l1 * lq + l2] += 16 * q / (3 * n);
           }
@@ -926,7 +992,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     const int nk = J.nk;
     double res;
     // FP64 integrand in every mode: the reference's test
-    bool ok = ps93_walk(J.wSmall, ws, we, J.tol, 0.0,
+    bool ok = ps93_walk_fast(J.wSmall, ws, we, J.tol,
                         [&](int n) {
                           return Fa[n * nF + l1] * Fb[n * nF + l2] * Ut[((size_t)n * LE + l) * nk + l3];
                         },
