@@ -55,7 +55,7 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
   const double *cf;
   int cs;
   if (asy) {
-    mult = 0.5 / z;
+    mult = 0.5 * __drcp_rn(z);  // = 0.5 / z exactly (scaling by 2^-1)
     x = -mult;
     cf = J.besA;
     cs = HL1 < 6 ? 6 : HL1;
@@ -346,6 +346,21 @@ static __device__ const double kRecip[25] = {0.0,        1.0,        1.0 / 2,  1
                                              1.0 / 10,   1.0 / 11,   1.0 / 12, 1.0 / 13, 1.0 / 14,
                                              1.0 / 15,   1.0 / 16,   1.0 / 17, 1.0 / 18, 1.0 / 19,
                                              1.0 / 20,   1.0 / 21,   1.0 / 22, 1.0 / 23, 1.0 / 24};
+
+// Binomial coefficients C(n, k), n <= 15, as exact doubles: the values
+// fac[n] / (fac[n-k] fac[k]) of src/util.c:247-334 (exact integers), looked
+// up instead of divided out per term.
+struct BinomTable {
+  double v[16][16];
+  constexpr BinomTable() : v() {
+    for (int n = 0; n < 16; n++) {
+      v[n][0] = 1.0;
+      for (int k = 1; k <= n; k++) v[n][k] = v[n - 1][k - 1] + (k < n ? v[n - 1][k] : 0.0);
+    }
+  }
+};
+static __device__ const BinomTable kBinom;
+static __device__ inline double binom_tab(int n, int k) { return __ldg(&kBinom.v[n][k]); }
 
 // Direction of the k-vector P as (cos theta, cos phi, sin phi), the values
 // src/util.c:75-106 and src/spherical_harmonics.c:16-114 produce through
@@ -925,11 +940,11 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       const int *ex = J.ijk + 3 * (NCUM(lpa - 1) + c1);
       double v = 0.0;
       for (int x = 0; x <= ex[0]; x++) {
-        double bx = binom(J.fac, ex[0], x);
+        double bx = binom_tab(ex[0], x);
         for (int y = 0; y <= ex[1]; y++) {
-          double by = bx * binom(J.fac, ex[1], y);
+          double by = bx * binom_tab(ex[1], y);
           for (int zz = 0; zz <= ex[2]; zz++) {
-            double bz = by * binom(J.fac, ex[2], zz);
+            double bz = by * binom_tab(ex[2], zz);
             double factor = bz * uA[((ex[0] - x) * D + (ex[1] - y)) * D + (ex[2] - zz)];
             if (fabs(factor) <= J.acc) continue;
             v += factor * chi[J.ijkIdx[(x * dd + y) * dd + zz] * ncb + q];
@@ -944,11 +959,11 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       const int *ex = J.ijk + 3 * (NCUM(lpb - 1) + c2);
       double v = 0.0;
       for (int x = 0; x <= ex[0]; x++) {
-        double bx = binom(J.fac, ex[0], x);
+        double bx = binom_tab(ex[0], x);
         for (int y = 0; y <= ex[1]; y++) {
-          double by = bx * binom(J.fac, ex[1], y);
+          double by = bx * binom_tab(ex[1], y);
           for (int zz = 0; zz <= ex[2]; zz++) {
-            double bz = by * binom(J.fac, ex[2], zz);
+            double bz = by * binom_tab(ex[2], zz);
             double factor = bz * uB[((ex[0] - x) * D + (ex[1] - y)) * D + (ex[2] - zz)];
             if (fabs(factor) <= J.acc) continue;
             factor *= norm;
