@@ -243,6 +243,61 @@ static __device__ bool ps93_walk_fast(const double *w, int start, int end, doubl
   return false;
 }
 
+// psm92_advance over the slots [s0, s1) whose bit is set in `bits`; the
+// other slots integrate to exactly zero, so (lower, upper) pairs without a set
+// bit are skipped -- adding 0.0 changes no sum -- while every level end is
+// still visited in order for the convergence test.
+template <class V, class Vis>
+static __device__ inline void psm92_sparse(int s0, int s1, const unsigned *bits, double tol, double rel, V val,
+                                           Vis vis, double &I, double &p, double &q, bool &done, double &res) {
+  auto has = [&](int t) { return (bits[t >> 5] >> (t & 31)) & 1u; };
+  int pos = s0;
+  if (pos == 0) {
+    I = has(0) ? val(0) : 0.0;
+    p = I;
+    pos = 1;
+  }
+  int k = level_of(pos);
+  while (pos < s1 && !done) {
+    const int lvStart = k == 0 ? 1 : c92_lvEnd[k - 1];
+    if (pos == lvStart) {
+      q = 2 * p;
+      p = 2 * I;
+    }
+    const int lvE = c92_lvEnd[k], stop = lvE < s1 ? lvE : s1;
+    while (true) {
+      int t = stop;  // first set bit in [pos, stop)
+      for (int w = pos >> 5; (w << 5) < stop; w++) {
+        unsigned word = bits[w];
+        if (w == (pos >> 5)) word &= ~0u << (pos & 31);
+        if (word) {
+          t = (w << 5) + __ffs(word) - 1;
+          break;
+        }
+      }
+      if (t >= stop) {
+        pos = stop;
+        break;
+      }
+      const int ps = (t - 1) | 1;  // the (lower, upper) pair holding t
+      double T = 0.0;
+      if (has(ps)) T += val(ps);
+      if (has(ps + 1) && vis(ps + 1)) T += val(ps + 1);
+      I += T;
+      pos = ps + 2;
+    }
+    if (pos == lvE) {
+      double N = c92_lvN[k] + 1.0, e = I - p;
+      const double t = rel > 0.0 && N >= kMixedMinPoints ? fmax(tol, rel * fabs(16 * I / (3 * N))) : tol;
+      if (16 * e * e <= 3 * N * fabs(I - q) * t) {
+        res = 16 * I / (3 * N);
+        done = true;
+      }
+      k++;
+    }
+  }
+}
+
 // --------------------------------------------------------------- layout
 
 // Quadratures per primitive pair in the type-1 block ((l1, l2), l2 = l1,
@@ -272,6 +327,7 @@ struct FastSmem {
   int w2Stride, w2Tab, w2I, w2P, w2Q, w2R, w2Part, tab2Stride;
   int w2Bits, w2Pend, w2Pref;  // fallback streaming: needed-slot bitmap, pending slots, word prefixes
   int ppMap;                   // type-2 fallback: FM06 map (i1, i2) of every primitive pair
+  int ppWin;                   // and the point-index interval where its exponent can pass the screen
 };
 
 __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap, int maxNP) {
@@ -316,7 +372,8 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap,
   s.w2Pref = s.w2Pend + 32;                   // kLargeWords int
   s.w2Stride = s.w2Pref + kLargeWords / 2;
   s.ppMap = kWarps * s.w2Stride;
-  int t2b = s.ppMap + 2 * maxNP;
+  s.ppWin = s.ppMap + 2 * maxNP;  // 2 ints per pair
+  int t2b = s.ppWin + maxNP;
   int ph = t1;
   if (t2a > ph) ph = t2a;
   if (t2b > ph) ph = t2b;
@@ -710,7 +767,8 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
 static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, const FastShared &S,
                                int k, int Nb, int nf, int c, int Lc, int la, int lb, const double *pzA,
                                const double *pcA, const double *pzB, const double *pcB, double dAC,
-                               double dBC, int ncls, int pa0, int pb0, const double *map, int &warn) {
+                               double dBC, int ncls, int pa0, int pb0, const double *map, const int *win,
+                               int &warn) {
   const int lane = threadIdx.x & 31, nA = 2 * J.maxLBS + 1;
   const int LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE, OL = J.largeOrder;
   const int TS = L.tab2Stride;
@@ -722,8 +780,14 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
   // derivative blocks: the product times zeta_a^max(0, shifta), then
   // zeta_b^max(0, shiftb) (src/type2.c:456-462)
   const double Ck = zeta_times(zeta_times(ca * cb, za, pa0), zb, pb0);
-  const double i1 = map[2 * k];
+  const double i1 = map[2 * k], i2 = map[2 * k + 1];
   const int nb = S.ppBreak[k], end = nb == INT_MAX ? OL - 1 : nb - 1;
+  const int nLo = win[2 * k], nHi = win[2 * k + 1];
+  // the latest break of the earlier pairs: beyond it no earlier pair's
+  // buffers are reused
+  int mb = -1;
+  for (int j = lane; j < k; j += 32) mb = S.ppBreak[j] > mb ? S.ppBreak[j] : mb;
+  mb = __reduce_max_sync(0xffffffffu, mb);
   for (int q = lane; q < nf; q += 32) { sI[q] = 0; sP[q] = 0; sQ[q] = 0; sR[q] = 0; }
   for (int w = lane; w < (OL + 31) / 32; w += 32) needBits[w] = 0u;
   __syncwarp();
@@ -763,10 +827,19 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       const int c1 = step_end92(cpos) < OL ? step_end92(cpos) : OL, t = cpos + lane;
       bool need = false;
       if (t < c1) {
-        int owner;
-        double r, ex;
-        locate(t, owner, r, ex);
-        need = owner >= 0 && ex >= J.lnAcc2;
+        const int n = __ldg(J.s92 + t);
+        if (n < nb) {
+          // this pair's own point: only inside its interval can the exponent pass
+          if (n >= nLo && n <= nHi) {
+            const double r = i1 * J.xLarge[n] + i2, d1 = dAC - r, d2 = dBC - r;
+            need = -za * d1 * d1 - zb * d2 * d2 >= J.lnAcc2;
+          }
+        } else if (n <= mb && n != nb && !(t > 0 && ((t - 1) & 1))) {
+          int owner;
+          double r, ex;
+          locate(t, owner, r, ex);
+          need = owner >= 0 && ex >= J.lnAcc2;
+        }
       }
       const unsigned m = __ballot_sync(0xffffffffu, need);
       if (need) {
@@ -821,17 +894,16 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       while (qq >= J.itemCnt[ncls + l]) { qq -= J.itemCnt[ncls + l]; l++; }
       int it = J.items[J.itemOff[ncls + l] + qq];
       int l1 = it & 255, l2 = (it >> 8) & 255, l3 = it >> 16;
-      auto val = [&](int t) {
+      auto val = [&](int t) {  // a queued slot
         const unsigned word = needBits[t >> 5], bit = 1u << (t & 31);
-        if (!(word & bit)) return 0.0;
         const double *e = tab + (pref[t >> 5] + __popc(word & (bit - 1u))) * TS;
         const double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
         return Ka[l1] * Kb[l2] * U[l] * R[l3];
       };
-      auto vis = [&](int t) { return !(t > 0 && ((t - 1) & 1)) || c92_slot[t] <= end; };
+      auto vis = [&](int t) { return c92_slot[t] <= end; };  // an upper slot
       double I = sI[q], p = sP[q], qv = sQ[q], res = 0;
       bool done = false;
-      psm92_advance(wpos, b, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
+      psm92_sparse(wpos, b, needBits, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
       sI[q] = I; sP[q] = p; sQ[q] = qv;
       if (done) { sR[q] = res; doneBits[qi] |= 1u << lane; }
       else {
@@ -1020,6 +1092,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     // break index of every primitive pair (bisection: the break predicate is
     // monotone in the index beyond both centres)
     double *map = ph + Lm.ppMap;  // (the small-grid stage's F tables are no longer read)
+    int *win = (int *)(ph + Lm.ppWin);
     for (int k = tid; k < NP; k += NT) {
       double za = pzA[k / Nb], zb = pzB[k % Nb], i1, i2;
       fm06(za, zb, dAC, dBC, i1, i2);
@@ -1033,6 +1106,34 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
         if (r > dAC && r > dBC && e < J.lnAcc2) hi = mid; else lo = mid + 1;
       }
       S.ppBreak[k] = lo < J.largeOrder ? lo : INT_MAX;
+      // point-index interval outside which this pair's exponent stays below
+      // the screen by a margin of 1: the exponent is a parabola in r with
+      // its vertex at P and r grows with the index
+      const double thr = J.lnAcc2 - 1.0, P = (za * dAC + zb * dBC) / (za + zb);
+      auto exq = [&](int n) {
+        const double r = i1 * J.xLarge[n] + i2, d1 = dAC - r, d2 = dBC - r;
+        return -za * d1 * d1 - zb * d2 * d2;
+      };
+      int a = 0, bb = J.largeOrder;
+      while (a < bb) {
+        const int mid = (a + bb) >> 1;
+        if (i1 * J.xLarge[mid] + i2 >= P) bb = mid; else a = mid + 1;
+      }
+      const int nv = a;
+      a = 0;
+      bb = nv;
+      while (a < bb) {
+        const int mid = (a + bb) >> 1;
+        if (exq(mid) >= thr) bb = mid; else a = mid + 1;
+      }
+      win[2 * k] = a;
+      a = nv;
+      bb = J.largeOrder;
+      while (a < bb) {
+        const int mid = (a + bb) >> 1;
+        if (exq(mid) < thr) bb = mid; else a = mid + 1;
+      }
+      win[2 * k + 1] = a - 1;
     }
     if (tid == 0) S.nextBase = 0;
     __syncthreads();
@@ -1065,7 +1166,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       __syncwarp();
       for (int k = warp; k < NP; k += kWarps)
         t2_pair(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0, ph + Lm.ppMap,
-                warn2);
+                (const int *)(ph + Lm.ppWin), warn2);
       __syncthreads();
       for (int q = tid; q < nf; q += NT) {
         double v = 0.0;
