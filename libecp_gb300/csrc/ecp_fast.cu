@@ -321,8 +321,6 @@ struct FastSmem {
   int chi, J, T, phase, total;
   // type-1 per warp (inside phase): pair scalars, S_lm, Q, H, step table
   int w1Stride, w1Sc, w1Rsh, w1Q, w1H, w1Tab;
-  // type-2: small-grid stage (inside phase)
-  int Fa, Fb;
   // type-2 fallback per warp (inside phase)
   int w2Stride, w2Tab, w2I, w2P, w2Q, w2R, w2Part, tab2Stride;
   int w2Bits, w2Pend, w2Pref;  // fallback streaming: needed-slot bitmap, pending slots, word prefixes
@@ -356,9 +354,6 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap,
   s.w1Tab = s.w1H + ncAB;
   s.w1Stride = s.w1Tab + tt;
   int t1 = kWarps * s.w1Stride;
-  s.Fa = 0;
-  s.Fb = kSmallOrder * nF;
-  int t2a = 2 * kSmallOrder * nF;
   // type 2 fallback: 32-slot table (w, base, vis, U[nE], R[nA], Ka[LBE], Kb[LBE]) + walker state
   s.tab2Stride = (3 + nE + nA + 2 * LBE) | 1;  // odd: conflict-free lane strides
   s.w2Tab = 0;
@@ -375,7 +370,6 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap,
   s.ppWin = s.ppMap + 2 * maxNP;  // 2 ints per pair
   int t2b = s.ppWin + maxNP;
   int ph = t1;
-  if (t2a > ph) ph = t2a;
   if (t2b > ph) ph = t2b;
   s.total = s.phase + ph;
   return s;
@@ -390,6 +384,7 @@ struct FastShared {
   int failIdx[kWalkCap];
   unsigned failMask[64];
   int nFail, nThis, nextBase;
+  int t2Next;                   // next small-grid item to hand out
   unsigned passMask;            // channels read by this pass's failed quadratures
   int passL1, passL2, passL3;   // highest Ka, Kb and r^l rows they read
   int warn;
@@ -975,7 +970,46 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   double *out1 = J.out + (size_t)c * J.centreStride + J.pairOff[pr];
   double *out2 = out1 + NCART(lpa) * NCART(lpb);
   int warn1 = 0, warn2 = 0;
-  if (tid == 0) S.warn = 0;
+  // type-2 small-grid quadratures (src/type2.c:337-387): the items of the
+  // unit's class, their F tables (derivative runs max(0, shift),
+  // src/type2.c:563-564) and r^k U_l table read through L2
+  const int nF = J.nF, nk = J.nk;
+  const int nRuns = J.nRuns > 0 ? J.nRuns : 1;
+  const double *gFa = J.F + (((size_t)c * J.nShells + sa) * nRuns + pa0) * O * nF;
+  const double *gFb = J.F + (((size_t)c * J.nShells + sb) * nRuns + pb0) * O * nF;
+  const double *Ut = J.utab + (size_t)c * O * LE * nk;
+  const int ncls = (la * (J.maxLBS + 1) + lb) * LE;
+  int nItems = 0;
+  for (int l = 0; l < Lc; l++) nItems += J.itemCnt[ncls + l];
+  auto item = [&](int q, int &l, int &l1, int &l2, int &l3) {
+    l = 0;
+    while (q >= J.itemCnt[ncls + l]) { q -= J.itemCnt[ncls + l]; l++; }
+    int v = J.items[J.itemOff[ncls + l] + q];
+    l1 = v & 255; l2 = (v >> 8) & 255; l3 = v >> 16;
+  };
+  auto tidx = [&](int l, int l1, int l2, int l3) { return ((l * LBE + l1) * LBE + l2) * nA + l3; };
+  auto small_item = [&](int q) {
+    int l, l1, l2, l3;
+    item(q, l, l1, l2, l3);
+    double res;
+    // FP64 integrand in every mode: the reference's test
+    const bool ok = ps93_walk_fast(J.wSmall, ws, we, J.tol,
+                                   [&](int n) {
+                                     return __ldg(gFa + n * nF + l1) * __ldg(gFb + n * nF + l2) *
+                                            __ldg(Ut + ((size_t)n * LE + l) * nk + l3);
+                                   },
+                                   res);
+    if (ok) T[tidx(l, l1, l2, l3)] = res;
+    else { atomicOr(&S.failMask[q >> 5], 1u << (q & 31)); atomicAdd(&S.nFail, 1); }
+  };
+  for (int e = tid; e < LE * LBE * LBE * nA; e += NT) T[e] = 0.0;
+  for (int e = tid; e < 64; e += NT) S.failMask[e] = 0;
+  if (tid == 0) {
+    S.warn = 0;
+    S.nFail = 0;
+    S.t2Next = 0;
+  }
+  __syncthreads();
 
   // ---------------------------------------------------------- type 1
   {
@@ -992,6 +1026,16 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     for (int p0 = warp * G; p0 < NP; p0 += kWarps * G)
       t1_group_run(J, Lm, W, c, Lc, la, lb, p0, NP - p0 < G ? NP - p0 : G, Nb, pzA, pcA, pzB, pcB, gA, gB,
                    ws, we, pa0, pb0, warn1);
+    // the type-2 small-grid quadratures, 32 at a time to whichever warp is
+    // through with its type-1 groups (each writes its own entry of T: the
+    // result does not depend on the warp)
+    for (;;) {
+      int q0 = 0;
+      if ((tid & 31) == 0) q0 = atomicAdd(&S.t2Next, 32);
+      q0 = __shfl_sync(0xffffffffu, q0, 0);
+      if (q0 >= nItems) break;
+      if (q0 + (tid & 31) < nItems) small_item(q0 + (tid & 31));
+    }
     __syncthreads();
     // chi[i][j] = sum over warps of H[index(a_i + b_j)]
     const int dd = J.tmDim + 1;
@@ -1051,47 +1095,11 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   poly_shift(norm1, out1);
 
   // ---------------------------------------------------------- type 2
-  const int nF = J.nF;
-  double *Fa = ph + Lm.Fa, *Fb = ph + Lm.Fb;
-  // F tables of the derivative runs max(0, shift) (src/type2.c:563-564)
-  const int nRuns = J.nRuns > 0 ? J.nRuns : 1;
-  const double *gFa = J.F + (((size_t)c * J.nShells + sa) * nRuns + pa0) * O * nF;
-  const double *gFb = J.F + (((size_t)c * J.nShells + sb) * nRuns + pb0) * O * nF;
-  for (int e = tid; e < O * nF; e += NT) { Fa[e] = gFa[e]; Fb[e] = gFb[e]; }
-  for (int e = tid; e < LE * LBE * LBE * nA; e += NT) T[e] = 0.0;
-  for (int e = tid; e < 64; e += NT) S.failMask[e] = 0;
-  if (tid == 0) S.nFail = 0;
-  __syncthreads();
-  const double *Ut = J.utab + (size_t)c * O * LE * J.nk;
-  const int ncls = (la * (J.maxLBS + 1) + lb) * LE;
-  int nItems = 0;
-  for (int l = 0; l < Lc; l++) nItems += J.itemCnt[ncls + l];
-  auto item = [&](int q, int &l, int &l1, int &l2, int &l3) {
-    l = 0;
-    while (q >= J.itemCnt[ncls + l]) { q -= J.itemCnt[ncls + l]; l++; }
-    int v = J.items[J.itemOff[ncls + l] + q];
-    l1 = v & 255; l2 = (v >> 8) & 255; l3 = v >> 16;
-  };
-  auto tidx = [&](int l, int l1, int l2, int l3) { return ((l * LBE + l1) * LBE + l2) * nA + l3; };
-  for (int q = tid; q < nItems; q += NT) {  // small-grid PS93 (src/type2.c:337-387)
-    int l, l1, l2, l3;
-    item(q, l, l1, l2, l3);
-    const int nk = J.nk;
-    double res;
-    // FP64 integrand in every mode: the reference's test
-    bool ok = ps93_walk_fast(J.wSmall, ws, we, J.tol,
-                        [&](int n) {
-                          return Fa[n * nF + l1] * Fb[n * nF + l2] * Ut[((size_t)n * LE + l) * nk + l3];
-                        },
-                        res);
-    if (ok) T[tidx(l, l1, l2, l3)] = res;
-    else { atomicOr(&S.failMask[q >> 5], 1u << (q & 31)); atomicAdd(&S.nFail, 1); }
-  }
-  __syncthreads();
+  // (the small-grid quadratures ran beside the type-1 groups)
   if (S.nFail > 0) {
     // break index of every primitive pair (bisection: the break predicate is
     // monotone in the index beyond both centres)
-    double *map = ph + Lm.ppMap;  // (the small-grid stage's F tables are no longer read)
+    double *map = ph + Lm.ppMap;
     int *win = (int *)(ph + Lm.ppWin);
     for (int k = tid; k < NP; k += NT) {
       double za = pzA[k / Nb], zb = pzB[k % Nb], i1, i2;
