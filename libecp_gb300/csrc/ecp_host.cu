@@ -196,8 +196,10 @@ int parse_system(const ecpgb_system &s, Parsed &P) {
   P.largeGridOrder = s.largeGridOrder;
   P.tol = s.tolerance;
   P.acc = s.accuracy;
-  if (s.largeGridOrder < 384 || s.largeGridOrder >= 2 * (kMaxLargeOrder + 1)) {
-    set_error("largeGridOrder %d outside 384..%d", s.largeGridOrder, 2 * (kMaxLargeOrder + 1) - 1);
+  // the grid has 2^floor(log2(order + 1)) - 1 points: at most kMaxLargeOrder
+  // up to order 2 (kMaxLargeOrder + 1) - 2
+  if (s.largeGridOrder < 384 || s.largeGridOrder > 2 * (kMaxLargeOrder + 1) - 2) {
+    set_error("largeGridOrder %d outside 384..%d", s.largeGridOrder, 2 * (kMaxLargeOrder + 1) - 2);
     return 1;
   }
   if (!(s.accuracy > 0) || !(s.tolerance > 0)) {

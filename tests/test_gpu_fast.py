@@ -64,6 +64,19 @@ def test_fast_where_reference_aborts_and_forced_failures(eg):
     assert_blocks_match(meta, data, mo, do)
 
 
+@pytest.mark.parametrize("order", [2048, 8190])
+def test_fast_other_parameters(eg, order):
+    """Large grids of 2047 and 4095 points, looser tolerance, other accuracy,
+    non-integer r^n, contraction up to 8 (break searches over several
+    chunks, the widest fallback bitmaps)."""
+    s = W.random_system(23, n_atoms=3, n_centres=2, lmax_basis=2, lmax_ecp=3, kmax=8)
+    s.nECP[::3] += 0.5
+    s.largeGridOrder, s.tolerance, s.accuracy = order, 1e-10, 1e-12
+    rc, mo, do = O.oracle_blocks(s)
+    meta, data = eg.blocks(s, mode=eg.ECPGB_FAST)
+    assert_blocks_match(meta, data, mo, do)
+
+
 def test_fast_maximum_sizes(eg):
     rng = np.random.default_rng(5)
     b = W._Builder()
