@@ -51,8 +51,8 @@ sys.path.insert(0, ROOT)
 METRIC = "ECP shell-pair integrals/s"
 UNIT = "integrals/s"
 WORKLOAD = "batched_cluster: 50 ECP centres x 2016 shell pairs (63 shells, l<=3, K 1-8), FP64"
+
 # Algorithmic FLOP weights of the reference control flow, counted by the oracle:
-# Algorithmic FLOP weights of the reference control flow:
 # 4 per quadrature point, Bessel 30 per row + 80 per call, exp 20, table 3 per
 # row, 2 per contraction multiply-add.
 def algorithmic_flops(st: dict) -> float:
