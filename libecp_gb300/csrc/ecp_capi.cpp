@@ -35,6 +35,24 @@ struct ecpgb_job {
   void *impl;
 };
 
+namespace {
+
+// The engine behind the reference's own entry points (getIntegrals,
+// calculateECPIntegrals): the plain FP64 kernels unless the environment
+// variable LIBECP_GB300_MODE selects the batched FP64 engine ("fast": the
+// same results within 1e-10, several times faster) or the mixed-precision
+// mode ("mixed"), so that a host program linked unchanged can switch.
+int drop_in_mode() {
+  const char *m = std::getenv("LIBECP_GB300_MODE");
+  if (!m || !*m || !std::strcmp(m, "fp64")) return ECPGB_FP64;
+  if (!std::strcmp(m, "fast")) return ECPGB_FAST;
+  if (!std::strcmp(m, "mixed")) return ECPGB_MIXED;
+  fprintf(stderr, "libecp_gb300: LIBECP_GB300_MODE=%s is not fp64, fast or mixed; using fp64\n", m);
+  return ECPGB_FP64;
+}
+
+}  // namespace
+
 extern "C" {
 
 int getIntegrals(int nrAtoms, double *geometry, int *shellsECP, int *KECP, int *lECP, double *nECP,
@@ -43,7 +61,7 @@ int getIntegrals(int nrAtoms, double *geometry, int *shellsECP, int *KECP, int *
                  double *I) {
   ecpgb_system s = {nrAtoms, geometry, shellsECP, KECP, lECP, nECP, dECP, aECP,
                     shellsBS, lBS, KBS, dBS, aBS, largeGridOrder, tolerance, accuracy};
-  int rc = ecpgb::run_matrix(s, ECPGB_FP64, rowdim, I, nullptr);
+  int rc = ecpgb::run_matrix(s, drop_in_mode(), rowdim, I, nullptr);
   if (rc == 1 || rc < 0) {
     printf("error initializing libECP\n");
     fprintf(stderr, "libecp_gb300: %s\n", ecpgb::last_error());
@@ -106,7 +124,7 @@ int calculateECPIntegrals(libECPHandle *h, ECPCallback cb, void *args) {
   std::vector<int> status(nUnits > 0 ? nUnits : 1);
   ecpgb_info info;
   ecpgb::Parsed P;
-  if (ecpgb::run_blocks(h->sys, ECPGB_FP64, values.data(), offsets.data(), status.data(), &info, &P)) {
+  if (ecpgb::run_blocks(h->sys, drop_in_mode(), values.data(), offsets.data(), status.data(), &info, &P)) {
     fprintf(stderr, "libecp_gb300: %s\n", ecpgb::last_error());
     return -1;
   }

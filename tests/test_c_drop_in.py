@@ -60,3 +60,29 @@ def test_matches_python_binding(tmp_path):
         off += (m[2] + 1) * (m[2] + 2) // 2 * ((m[5] + 1) * (m[5] + 2) // 2)
     cb = [float(l.split()[-1]) for l in out if l.startswith("B ")]
     assert np.array_equal(np.array(cb), np.array(firsts))
+
+
+@pytest.mark.gpu
+def test_environment_selects_the_batched_engine(tmp_path):
+    """LIBECP_GB300_MODE=fast: the unchanged host program runs on the batched
+    engine; its matrix and callback blocks agree with the default run within
+    the FP64 bar."""
+    exe = build(tmp_path)
+
+    def run(mode):
+        env = dict(os.environ)
+        if mode is None:
+            env.pop("LIBECP_GB300_MODE", None)
+        else:
+            env["LIBECP_GB300_MODE"] = mode
+        out = subprocess.run([exe], capture_output=True, text=True, check=True, env=env)
+        return out.stdout.splitlines(), out.stderr
+
+    base, _ = run(None)
+    fast, _ = run("fast")
+    assert "RC 0" in fast and "CB 0" in fast
+    vals = lambda out: np.array([float(l.split()[-1]) for l in out if l.startswith(("M ", "B "))])
+    assert len(vals(base)) == len(vals(fast)) > 0
+    assert np.max(np.abs(vals(base) - vals(fast))) <= 1e-10
+    bad, err = run("bogus")
+    assert "not fp64, fast or mixed" in err and "RC 0" in bad
