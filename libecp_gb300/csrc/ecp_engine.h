@@ -190,7 +190,7 @@ int launch_fp64_pipeline(const DevJob &job, cudaStream_t stream, size_t smemByte
                          cudaEvent_t u1);
 // The four per-job kernels before the unit kernel (radii, centre potentials,
 // centre-atom angular tables, windows + F tables) and the AO scatter after it.
-void launch_prologue(const DevJob &job, cudaStream_t stream);
+void launch_prologue(const DevJob &job, cudaStream_t stream, bool withF);
 void launch_epilogue(const DevJob &job, cudaStream_t stream);
 
 // Batched path (ecp_fast.cu): same prologue/epilogue, warp-per-primitive-pair

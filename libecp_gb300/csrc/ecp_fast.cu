@@ -1230,6 +1230,56 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   }
 }
 
+// The screening window and F table of every (shell, centre) -- k_shell_F of
+// the drop-in path (src/type2.c:223-310, src/type2.c:149-180) with the
+// batched path's Bessel rows and exp; FP64 in every mode.
+__global__ void __launch_bounds__(128) k_shell_F_fast(DevJob J) {
+  __shared__ int sw[3];
+  const int s = blockIdx.x, c = blockIdx.y, O = kSmallOrder;
+  const int C = J.ctrAtom[c], A = J.shAtom[s];
+  const double *rC = J.geom + 3 * C, *rA = J.geom + 3 * A;
+  double x = rC[0] - rA[0], y = rC[1] - rA[1], z = rC[2] - rA[2];
+  const double dAC = sqrt(x * x + y * y + z * z);
+  if (threadIdx.x == 0) {
+    int end = J.gridEnd[c], j;
+    double R = J.radius[s], rmin = dAC - R, rmax = dAC + R;
+    for (j = end; j >= 0; j--)
+      if (J.xSmall[j] < rmin) break;
+    sw[0] = j + 1;
+    for (j = end; j >= 0; j--)
+      if (J.xSmall[j] <= rmax) break;
+    sw[1] = (j < 0 || J.xSmall[j] > rmax) ? -1 : j;
+    sw[2] = !(sw[1] >= sw[0]) || R < 0;
+    int *w = J.win + ((size_t)c * J.nShells + s) * 3;
+    w[0] = sw[0]; w[1] = sw[1]; w[2] = sw[2];
+  }
+  __syncthreads();
+  // run = derivative order of the table: rows up to L - 1 + l + run and
+  // coefficients times zeta^run (src/type2.c:229, :263-290)
+  const int nF = J.nF, nRuns = J.nRuns > 0 ? J.nRuns : 1;
+  const double *pa = J.primA + J.shP[s], *pd = J.primD + J.shP[s];
+  for (int run = 0; run < nRuns; run++) {
+    const int lmaxA = J.maxLECP - 1 + J.shL[s] + run;
+    double *F = J.F + (((size_t)c * J.nShells + s) * nRuns + run) * O * nF;
+    for (int n = threadIdx.x; n < O; n += blockDim.x) {
+      double acc[kMaxRows], K[kMaxRows];
+      for (int i = 0; i < nF; i++) acc[i] = 0.0;
+      if (!sw[2] && n >= sw[0] && n < sw[1] && lmaxA >= 0) {
+        double r = J.xSmall[n];
+        for (int p = 0; p < J.shK[s]; p++) {
+          double zeta = pa[p], da = pd[p];
+          for (int k = 0; k < run; k++) da *= zeta;
+          bessel_fast(J, lmaxA, 2.0 * zeta * dAC * r, K, 1);
+          double e = dAC - r;
+          e = fast_exp(-zeta * e * e);
+          for (int i = 0; i <= lmaxA; i++) acc[i] += da * K[i] * e;
+        }
+      }
+      for (int i = 0; i < nF; i++) F[(size_t)n * nF + i] = acc[i];
+    }
+  }
+}
+
 // The unit at queue position i (cost order, or the reference's order).
 __device__ inline long long queue_unit(const DevJob &J, long long i) { return J.order ? J.order[i] : i; }
 
@@ -1389,7 +1439,12 @@ int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, con
   if (!cfg.sorted) Jc.order = nullptr;
   const bool screen = cfg.queue && cfg.screen && J.queueHead && J.live && J.liveCount && J.screenBlocks;
   if (!screen) Jc.live = nullptr;
-  launch_prologue(Jc, st);
+  launch_prologue(Jc, st, false);
+  {
+    DevJob Jf = Jc;
+    Jf.mixed = 0;  // the F tables stay FP64 in every mode
+    k_shell_F_fast<<<dim3(J.nShells, J.nCentres), 128, 0, st>>>(Jf);
+  }
   long long nUnits = (long long)J.nCentres * J.nPairs;
   if (screen && nUnits > 0) {  // screening stage: the queue of live units
     const long long nb = (nUnits + kScreenThreads - 1) / kScreenThreads;

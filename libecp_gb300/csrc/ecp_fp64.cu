@@ -732,7 +732,7 @@ int launch_fp64_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, cud
     attr[dev] = true;
   }
   if (smemBytes > 200 * 1024) return 3;
-  launch_prologue(J, st);
+  launch_prologue(J, st, true);
   long long nUnits = (long long)J.nCentres * J.nPairs;
   if (u0) record_timing(u0, st);
   if (nUnits > 0) k_unit<<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(J);
@@ -742,12 +742,13 @@ int launch_fp64_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, cud
   return e == cudaSuccess ? 0 : kLaunchErrorBase + (int)e;
 }
 
-// Per-job stages before and after the unit kernel; shared by both paths.
-void launch_prologue(const DevJob &J, cudaStream_t st) {
+// Per-job stages before and after the unit kernel; shared by both paths
+// (the batched path launches its own F-table kernel: withF false).
+void launch_prologue(const DevJob &J, cudaStream_t st, bool withF) {
   k_radius<<<(J.nShells + 127) / 128, 128, 0, st>>>(J);
   k_centre<<<J.nCentres, 128, sizeof(double) * kSmallOrder * (kMaxLEcp + 1), st>>>(J);
   k_centre_atom<<<dim3(J.nAtoms, J.nCentres), 64, 0, st>>>(J);
-  k_shell_F<<<dim3(J.nShells, J.nCentres), 128, 0, st>>>(J);
+  if (withF) k_shell_F<<<dim3(J.nShells, J.nCentres), 128, 0, st>>>(J);
 }
 
 void launch_epilogue(const DevJob &J, cudaStream_t st) {
