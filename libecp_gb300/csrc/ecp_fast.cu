@@ -48,6 +48,7 @@ constexpr int kMixedMinPoints = 63;
 // large-argument polynomial, so that lanes on either branch run the same
 // instructions: row l is a polynomial of degree max(5, l) whose coefficients
 // above the branch's own degree are zero.
+template <bool kMixed>
 static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *K, int stride) {
   if (z < 1.0E-7) {
     bessel_eval(J, lmax, z, K, stride);
@@ -67,7 +68,7 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
     const double h = J.besselN / 16;  // integer division, as the reference
     const int index = (int)floor(z * h + 0.5);
     x = z - __ldg(J.besZ + index);  // index / h, tabulated
-    if (J.mixed) {
+    if constexpr (kMixed) {
       // mixed mode: the Taylor rows in FP32 (every lane of the warp is on
       // this branch or the large-argument one, which stays FP64)
       const float *qf = J.besHf + (size_t)index * HL1 * 6;
@@ -130,37 +131,40 @@ static __device__ inline float term_f32(const DevJob &J, int t, float r, float r
 
 // U_l(r) of centre c for the channels l set in mask, in one pass over its
 // terms (src/ecp.c:42-60); the other entries of U are left untouched.
+template <bool kMixed>
 static __device__ void channels_masked(const DevJob &J, int c, double r, unsigned mask, double *U) {
   double r2 = r * r;
   for (unsigned m = mask; m; m &= m - 1) U[__ffs(m) - 1] = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
-  if (J.mixed) {
+  if constexpr (kMixed) {
     const float rf = (float)r, r2f = (float)r2;
     for (int t = t0; t < t1; t++) {
       int l = J.termL[t];
       if (mask >> l & 1u) U[l] += (double)term_f32(J, t, rf, r2f);
     }
-    return;
-  }
-  for (int t = t0; t < t1; t++) {
-    int l = J.termL[t];
-    if (mask >> l & 1u) U[l] += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
+  } else {
+    for (int t = t0; t < t1; t++) {
+      int l = J.termL[t];
+      if (mask >> l & 1u) U[l] += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
+    }
   }
 }
 
+template <bool kMixed>
 static __device__ double channel(const DevJob &J, int c, int l, double r) {
   double r2 = r * r, pot = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
-  if (J.mixed) {
+  if constexpr (kMixed) {
     const float rf = (float)r, r2f = (float)r2;
     float pf = 0.0f;
     for (int t = t0; t < t1; t++)
       if (J.termL[t] == l) pf += term_f32(J, t, rf, r2f);
     return (double)pf;
+  } else {
+    for (int t = t0; t < t1; t++)
+      if (J.termL[t] == l) pot += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
+    return pot;
   }
-  for (int t = t0; t < t1; t++)
-    if (J.termL[t] == l) pot += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
-  return pot;
 }
 
 // FM06 map parameters (src/gc_integrators.c:317-331).
@@ -488,13 +492,14 @@ static __device__ void rsh_column(const DevJob &J, int lmax, int m, double x, do
 // A group of G primitive pairs (p0 .. p0+G-1) of the type-1 block, by one
 // warp (src/type1.c:95-302); lane = (pair, quadrature).  Adds the group's terms
 // to the warp's per-combined-index accumulators H.
+template <bool kMixed>
 static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *W, int c, int Lc,
                                     int la, int lb, int p0, int G, int Nb, const double *pzA,
                                     const double *pcA, const double *pzB, const double *pcB,
                                     const double *gA, const double *gB, int ws, int we, int pa0, int pb0,
                                     int &warn) {
   const int lane = threadIdx.x & 31, lab = la + lb, lq = lab + 1, O = kSmallOrder;
-  const double rel = J.mixed ? kMixedRel : 0.0;
+  const double rel = kMixed ? kMixedRel : 0.0;
   // odd entry strides: lanes touching neighbouring entries hit distinct banks
   const int OL = J.largeOrder, TSs = 1 + 2 * lq, TSf = 3 + 2 * lq, RQ = lq * lq, nq = t1_items(lab);
   double *sc = W + L.w1Sc, *rsh = W + L.w1Rsh, *Q = W + L.w1Q, *H = W + L.w1H, *tab = W + L.w1Tab;
@@ -569,7 +574,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       double r = J.xSmall[n], ex = (sc[gg * 6 + 4] * r + s) * r;
       ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
       const double wB = J.wSmall[n] * (sc[gg * 6 + 3] * uL[n] * ex);
-      bessel_fast(J, lab, s * r, ent, 1);
+      bessel_fast<kMixed>(J, lab, s * r, ent, 1);
       double *WR = ent + lq, v = wB;
       WR[0] = v;
       for (int l = 1; l <= lab; l++) {
@@ -681,9 +686,9 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
         if (n < nb && !(upper && n > end)) {
           double r = i1 * J.xLarge[n] + i2, ex = (z * r + s) * r + zd2;
           if (ex >= J.lnAcc1) {
-            double v = w * (C2 * channel(J, c, Lc, r) * fast_exp(ex));
+            double v = w * (C2 * channel<kMixed>(J, c, Lc, r) * fast_exp(ex));
             any = v != 0.0;
-            bessel_fast(J, kq, s * r, K, 1);
+            bessel_fast<kMixed>(J, kq, s * r, K, 1);
             WR[0] = v;
             for (int l = 1; l <= rq; l++) {
               v *= r;
@@ -720,7 +725,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
           return e[lq + l1] * e[l2];
         };
         auto vis = [&](int t) { return c92_slot[t] <= end; };
-        psm92_advance(s0, s1, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I2, p2, q2, done2, res2);
+        psm92_advance(s0, s1, J.tol, kMixed ? kMixedRel : 0.0, val, vis, I2, p2, q2, done2, res2);
       }
       __syncwarp();
       s0 = s1;
@@ -763,6 +768,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
 // One primitive pair of the type-2 large-grid fallback, by one warp
 // (src/type2.c:418-528): integrates the pass's failed items and adds each
 // result to the warp's partial sums.
+template <bool kMixed>
 static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, const FastShared &S,
                                int k, int Nb, int nf, int c, int Lc, int la, int lb, const double *pzA,
                                const double *pcA, const double *pzB, const double *pcB, double dAC,
@@ -868,10 +874,10 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       // Ka rows carry the weight and prefactor: w * Ck * e^(..) * K_l1
       const double wB = (J.wLarge[n] * i1) * (Ck * fast_exp(ex));
       // only the channels and rows this pass's quadratures read
-      channels_masked(J, c, r, pMask, U);
-      bessel_fast(J, pL1, 2.0 * zaj * dAC * r, Ka, 1);
+      channels_masked<kMixed>(J, c, r, pMask, U);
+      bessel_fast<kMixed>(J, pL1, 2.0 * zaj * dAC * r, Ka, 1);
       for (int l = 0; l <= pL1; l++) Ka[l] *= wB;
-      bessel_fast(J, pL2, 2.0 * zbj * dBC * r, Kb, 1);
+      bessel_fast<kMixed>(J, pL2, 2.0 * zbj * dBC * r, Kb, 1);
       R[0] = 1.0;
       for (int l = 1; l <= pL3; l++) R[l] = r * R[l - 1];
     }
@@ -902,7 +908,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       auto vis = [&](int t) { return c92_slot[t] <= end; };  // an upper slot
       double I = sI[q], p = sP[q], qv = sQ[q], res = 0;
       bool done = false;
-      psm92_sparse(wpos, b, needBits, J.tol, J.mixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
+      psm92_sparse(wpos, b, needBits, J.tol, kMixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
       sI[q] = I; sP[q] = p; sQ[q] = qv;
       if (done) { sR[q] = res; doneBits[qi] |= 1u << lane; }
       else {
@@ -940,6 +946,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
 
 // One unit (centre c, shell pair pr) by the whole CTA.  Every thread enters
 // and leaves together (the early exits are CTA-uniform).
+template <bool kMixed>
 static __device__ void unit_fast(const DevJob &J, const long long u, FastShared &S, double *sm) {
   const int c = (int)(u / J.nPairs), pr = (int)(u % J.nPairs);
   const int sa = J.pairA[pr], sb = J.pairB[pr], tid = threadIdx.x, NT = blockDim.x;
@@ -1028,7 +1035,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       if (Gb < G) G = Gb > 0 ? Gb : 1;
     }
     for (int p0 = warp * G; p0 < NP; p0 += kWarps * G)
-      t1_group_run(J, Lm, W, c, Lc, la, lb, p0, NP - p0 < G ? NP - p0 : G, Nb, pzA, pcA, pzB, pcB, gA, gB,
+      t1_group_run<kMixed>(J, Lm, W, c, Lc, la, lb, p0, NP - p0 < G ? NP - p0 : G, Nb, pzA, pcA, pzB, pcB, gA, gB,
                    ws, we, pa0, pb0, warn1);
     // the type-2 small-grid quadratures, 32 at a time to whichever warp is
     // through with its type-1 groups (each writes its own entry of T: the
@@ -1177,7 +1184,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       for (int q = tid & 31; q < nf; q += 32) W[Lm.w2Part + q] = 0.0;
       __syncwarp();
       for (int k = warp; k < NP; k += kWarps)
-        t2_pair(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0, ph + Lm.ppMap,
+        t2_pair<kMixed>(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0, ph + Lm.ppMap,
                 (const int *)(ph + Lm.ppWin), warn2);
       __syncthreads();
       for (int q = tid; q < nf; q += NT) {
@@ -1269,7 +1276,7 @@ __global__ void __launch_bounds__(128) k_shell_F_fast(DevJob J) {
         for (int p = 0; p < J.shK[s]; p++) {
           double zeta = pa[p], da = pd[p];
           for (int k = 0; k < run; k++) da *= zeta;
-          bessel_fast(J, lmaxA, 2.0 * zeta * dAC * r, K, 1);
+          bessel_fast<false>(J, lmaxA, 2.0 * zeta * dAC * r, K, 1);
           double e = dAC - r;
           e = fast_exp(-zeta * e * e);
           for (int i = 0; i <= lmaxA; i++) acc[i] += da * K[i] * e;
@@ -1284,16 +1291,18 @@ __global__ void __launch_bounds__(128) k_shell_F_fast(DevJob J) {
 __device__ inline long long queue_unit(const DevJob &J, long long i) { return J.order ? J.order[i] : i; }
 
 // A CTA per unit; blockIdx.x is a queue position.
+template <bool kMixed>
 __global__ void __launch_bounds__(kUnitThreads, kUnitCtasPerSm) k_unit_fast(DevJob J) {
   extern __shared__ double sm[];
   __shared__ FastShared S;
   const long long i = blockIdx.x;
-  unit_fast(J, J.order ? (long long)J.order[i] : i, S, sm);
+  unit_fast<kMixed>(J, J.order ? (long long)J.order[i] : i, S, sm);
 }
 
 // Persistent CTAs (as many as fit on the GPU) pulling queue positions from
 // one counter: the costliest units start first and the cheap ones fill the
 // tail, whatever order the hardware would dispatch CTAs in.
+template <bool kMixed>
 __global__ void __launch_bounds__(kUnitThreads, kUnitCtasPerSm) k_unit_queue(DevJob J) {
   extern __shared__ double sm[];
   __shared__ FastShared S;
@@ -1305,7 +1314,7 @@ __global__ void __launch_bounds__(kUnitThreads, kUnitCtasPerSm) k_unit_queue(Dev
     __syncthreads();
     const long long i = next;
     if (i >= n) break;
-    unit_fast(J, J.live ? (long long)J.live[i] : queue_unit(J, i), S, sm);
+    unit_fast<kMixed>(J, J.live ? (long long)J.live[i] : queue_unit(J, i), S, sm);
     __syncthreads();  // shared state is rewritten by the next unit
   }
 }
@@ -1408,7 +1417,8 @@ void fast_prepare() {
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64 || attr[dev]) return;
-  for (const void *k : {(const void *)k_unit_fast, (const void *)k_unit_queue}) {
+  for (const void *k : {(const void *)k_unit_fast<false>, (const void *)k_unit_queue<false>,
+                        (const void *)k_unit_fast<true>, (const void *)k_unit_queue<true>}) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     // the whole unified L1/shared array as shared memory: three CTAs of
     // <= 72 KB per SM
@@ -1420,7 +1430,7 @@ void fast_prepare() {
 int fast_ctas_per_sm(size_t smemBytes, int queue) {
   fast_prepare();
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, queue ? (const void *)k_unit_queue : (const void *)k_unit_fast,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, queue ? (const void *)k_unit_queue<false> : (const void *)k_unit_fast<false>,
                                                     kUnitThreads, smemBytes) != cudaSuccess)
     return 0;
   return n;
@@ -1461,9 +1471,11 @@ int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, con
       int per = fast_ctas_per_sm(smemBytes, 1);
       long long grid = (long long)sms * (per > 0 ? per : 1);
       if (grid > nUnits) grid = nUnits;
-      k_unit_queue<<<(unsigned)grid, kUnitThreads, smemBytes, st>>>(Jc);
+      if (cfg.mixed) k_unit_queue<true><<<(unsigned)grid, kUnitThreads, smemBytes, st>>>(Jc);
+      else k_unit_queue<false><<<(unsigned)grid, kUnitThreads, smemBytes, st>>>(Jc);
     } else {
-      k_unit_fast<<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(Jc);
+      if (cfg.mixed) k_unit_fast<true><<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(Jc);
+      else k_unit_fast<false><<<(unsigned)nUnits, kUnitThreads, smemBytes, st>>>(Jc);
     }
   }
   if (u1) record_timing(u1, st);
