@@ -48,10 +48,22 @@ constexpr int kMixedMinPoints = 63;
 // large-argument polynomial, so that lanes on either branch run the same
 // instructions: row l is a polynomial of degree max(5, l) whose coefficients
 // above the branch's own degree are zero.
+// K_0..K_lmax(z) for z < 1e-7: the reference's zeroth-order branch,
+// K_l = (1 - z) z^l / (2l+1)!! by its recurrence (src/bessel.c:118-133).
+static __device__ void bessel_small(int lmax, double z, double *K, int stride) {
+  if (z <= 0) {
+    K[0] = 1.0;
+    for (int l = 1; l <= lmax; l++) K[l * stride] = 0.0;
+  } else {
+    K[0] = 1 - z;
+    for (int l = 1; l <= lmax; l++) K[l * stride] = K[(l - 1) * stride] * z / (2 * l + 1);
+  }
+}
+
 template <bool kMixed>
 static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *K, int stride) {
   if (z < 1.0E-7) {
-    bessel_eval(J, lmax, z, K, stride);
+    bessel_small(lmax, z, K, stride);
     return;
   }
   const bool asy = z >= 16.0;
@@ -103,12 +115,25 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
   }
 }
 
-// One row K_l(z).
+// One row K_l(z), by the same branches as bessel_fast.
 static __device__ double bessel_row(const DevJob &J, int l, double z) {
-  if (z < 1.0E-7 || z >= 16.0) {
-    double K[kMaxRows];
-    bessel_eval(J, l, z, K, 1);
-    return K[l];
+  if (z < 1.0E-7) {
+    if (z <= 0) return l == 0 ? 1.0 : 0.0;
+    double v = 1 - z;
+    for (int i = 1; i <= l; i++) v = v * z / (2 * i + 1);
+    return v;
+  }
+  if (z >= 16.0) {
+    const int HL1 = J.besHL + 1;
+    const double mult = 0.5 * __drcp_rn(z), x = -mult;
+    const double *q = J.besA + (size_t)l * (HL1 < 6 ? 6 : HL1);
+    int k = l > 5 ? l : 5;
+    double v = q[k];
+    while (k > 0) {
+      k--;
+      v = fma(v, x, q[k]);
+    }
+    return v * mult;
   }
   double h = J.besselN / 16;
   int index = (int)floor(z * h + 0.5);
