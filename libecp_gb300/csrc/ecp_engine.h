@@ -200,7 +200,7 @@ void launch_epilogue(const DevJob &job, cudaStream_t stream);
 int upload_schedules_fast(const int *s93slot, int s93n, const int *s93lvEnd, const int *s93lvJ,
                           const int *s93lvN, int s93levels, const int *s92slot, int s92n,
                           const int *s92lvEnd, const int *s92lvN, int s92levels, void *stream);
-size_t fast_smem_bytes(int LB, int LE, int nF, int gcap, int maxNP);
+size_t fast_smem_bytes(int LB, int LE, int gcap, int maxNP);
 // CTAs of the batched unit kernel resident per SM at smemBytes.
 int fast_ctas_per_sm(size_t smemBytes, int queue);
 // Sets the batched kernels' function attributes on the current device (call

@@ -361,7 +361,7 @@ struct FastSmem {
   int ppWin;                   // and the point-index interval where its exponent can pass the screen
 };
 
-__host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap, int maxNP) {
+__host__ __device__ inline FastSmem fast_layout(int LB, int LE, int cap, int maxNP) {
   FastSmem s{};
   const int nA = 2 * LB + 1, nE = LE > 0 ? LE : 1, LBE = LB + nE;
   const int nc = (LB + 1) * (LB + 2) * (LB + 3) / 6, nct = (LB + 1) * (LB + 2) / 2;
@@ -408,8 +408,8 @@ __host__ __device__ inline FastSmem fast_layout(int LB, int LE, int nF, int cap,
   return s;
 }
 
-size_t fast_smem_bytes(int LB, int LE, int nF, int cap, int maxNP) {
-  return sizeof(double) * (size_t)fast_layout(LB, LE, nF, cap, maxNP).total;
+size_t fast_smem_bytes(int LB, int LE, int cap, int maxNP) {
+  return sizeof(double) * (size_t)fast_layout(LB, LE, cap, maxNP).total;
 }
 
 struct FastShared {
@@ -900,9 +900,11 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       const double wB = (J.wLarge[n] * i1) * (Ck * fast_exp(ex));
       // only the channels and rows this pass's quadratures read
       channels_masked<kMixed>(J, c, r, pMask, U);
-      bessel_fast<kMixed>(J, pL1, 2.0 * zaj * dAC * r, Ka, 1);
+      // the rows of both centres through one copy of the Bessel code
+#pragma unroll 1
+      for (int side = 0; side < 2; side++)
+        bessel_fast<kMixed>(J, side ? pL2 : pL1, side ? 2.0 * zbj * dBC * r : 2.0 * zaj * dAC * r, side ? Kb : Ka, 1);
       for (int l = 0; l <= pL1; l++) Ka[l] *= wB;
-      bessel_fast<kMixed>(J, pL2, 2.0 * zbj * dBC * r, Kb, 1);
       R[0] = 1.0;
       for (int l = 1; l <= pL3; l++) R[l] = r * R[l - 1];
     }
@@ -991,7 +993,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     if (tid == 0) J.status[u] = kUnitSkipped;
     return;
   }
-  const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.nF, J.gcap, J.maxNP);
+  const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.gcap, J.maxNP);
   const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa] + sh.a, lb = J.shL[sb] + sh.b, lab = la + lb;
   const int lpa = sh.lpa, lpb = sh.lpb, pa0 = sh.a > 0 ? sh.a : 0, pb0 = sh.b > 0 ? sh.b : 0;
   const int nA = 2 * J.maxLBS + 1, LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE;

@@ -567,7 +567,7 @@ int run_pipeline(JobBuffers &B, const DevJob &J, int mode, cudaEvent_t u0, cudaE
   if (mode == ECPGB_FAST || mode == ECPGB_MIXED) {
     FastConfig c = cfg ? *cfg : engine().config_for(J.maxLBS, J.maxLECP);
     c.mixed = mode == ECPGB_MIXED;
-    rc = launch_fast_pipeline(J, stream, fast_smem_bytes(J.maxLBS, J.maxLECP, J.nF, c.gcap, J.maxNP), c, u0, u1);
+    rc = launch_fast_pipeline(J, stream, fast_smem_bytes(J.maxLBS, J.maxLECP, c.gcap, J.maxNP), c, u0, u1);
   } else {
     rc = launch_fp64_pipeline(J, stream, B.smem, u0, u1);
   }
@@ -988,7 +988,7 @@ int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials,
   FastConfig bestCfg = R->cfg;
   int n = 0;
   for (const FastConfig &c : cand) {
-    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap, R->J.maxNP), c.queue) < 1) continue;
+    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, c.gcap, R->J.maxNP), c.queue) < 1) continue;
     float tot = 0;
     for (int r = 0; r < 3; r++) {
       cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
@@ -1032,7 +1032,7 @@ int job_config(void *vj, const ecpgb_launch_config *cfg, ecpgb_launch_config *ou
     c.gcap = cfg->gcap;
     c.balance = cfg->balance ? 1 : 0;
     c.screen = cfg->screen ? 1 : 0;
-    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, R->J.nF, c.gcap, R->J.maxNP), c.queue) < 1) {
+    if (fast_ctas_per_sm(fast_smem_bytes(R->J.maxLBS, R->J.maxLECP, c.gcap, R->J.maxNP), c.queue) < 1) {
       set_error("configuration does not fit on an SM");
       return 1;
     }
