@@ -12,11 +12,21 @@
 //     after ~27 of 1023 points on average, the reference tabulates all 1023;
 //   * K_l(z) as one Horner pass over precomputed Taylor coefficients (the
 //     reference's 5-step derivative recurrence, done once per table point on
-//     the host); exp by the table-driven method of ecp_fastmath.h;
+//     the host); exp by the table-driven method of ecp_fastmath.h; no FP64
+//     divide or trigonometric call in the hot loops (tabulated abscissae and
+//     reciprocals, division-free convergence tests, the k-vector direction
+//     from ratios);
+//   * only what is read is computed: type-1 tabulation for the pairs with a
+//     quadrature still running, fallback rows for the quadratures still
+//     running, and in the type-2 fallback only the slots whose value passes
+//     the screen (a pair's own points through its index interval), walked
+//     pair by pair with the empty slot pairs skipped;
 //   * the type-1 block accumulated per combined Cartesian index: chi[i][j]
 //     depends on (i, j) only through the index of a_i + b_j
 //     (src/type1.c:323-345), so one accumulator per combined index receives
-//     exactly the terms the reference adds to each chi[i][j].
+//     exactly the terms the reference adds to each chi[i][j];
+//   * the precision mode a template parameter: the FP64 kernels carry no
+//     mixed-precision code (instruction fetch is one of the kernel's stalls).
 #include "ecp_device.cuh"
 #include "ecp_fastmath.h"
 

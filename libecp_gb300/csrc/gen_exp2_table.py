@@ -6,10 +6,12 @@
   for |n| < 2^21), L2 the nearest double to ln2/512 - L1;
   512/ln2 rounded to nearest.
 
-Run from anywhere: python libecp_gb300/csrc/gen_exp2_table.py
+Run from anywhere: python libecp_gb300/csrc/gen_exp2_table.py [output]
+(default output: ecp_exp2_table.h beside this script).
 """
 import math
 import os
+import sys
 
 import mpmath
 
@@ -40,7 +42,8 @@ def main() -> None:
     for i in range(0, N, 4):
         lines.append("    " + ", ".join(v.hex() for v in vals[i:i + 4]) + ", \\")
     lines.append("  }")
-    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ecp_exp2_table.h")
+    out = sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                                                             "ecp_exp2_table.h")
     with open(out, "w") as f:
         f.write("\n".join(lines) + "\n")
 
