@@ -8,8 +8,9 @@
 //     no CTA barrier inside the type-1 loop or the type-2 fallback;
 //   * level-granular tabulation: grid points are tabulated 32 schedule slots
 //     at a time (one slot per lane) and a primitive pair stops as soon as all
-//     its quadratures have converged -- the large-grid quadratures converge
-//     after ~27 of 1023 points on average, the reference tabulates all 1023;
+//     its quadratures have converged -- on the 50-centre cluster the type-2
+//     fallback's quadratures stop after ~280 of the 1023 large-grid slots,
+//     where the reference tabulates all 1023;
 //   * K_l(z) as one Horner pass over precomputed Taylor coefficients (the
 //     reference's 5-step derivative recurrence, done once per table point on
 //     the host); exp by the table-driven method of ecp_fastmath.h; no FP64
