@@ -75,6 +75,23 @@ static __device__ void bessel_eval(const DevJob &J, int lmax, double z, double *
   }
 }
 
+// Screening window [start, end) of shell s on centre c's small grid and
+// whether the shell is screened out entirely (src/type2.c:149-180), written
+// to J.win and to w[3]; dAC = |C - A|.  One thread computes it.
+static __device__ void shell_window(const DevJob &J, int s, int c, double dAC, int *w) {
+  int end = J.gridEnd[c], j;
+  double R = J.radius[s], rmin = dAC - R, rmax = dAC + R;
+  for (j = end; j >= 0; j--)
+    if (J.xSmall[j] < rmin) break;
+  w[0] = j + 1;
+  for (j = end; j >= 0; j--)
+    if (J.xSmall[j] <= rmax) break;
+  w[1] = (j < 0 || J.xSmall[j] > rmax) ? -1 : j;
+  w[2] = !(w[1] >= w[0]) || R < 0;
+  int *g = J.win + ((size_t)c * J.nShells + s) * 3;
+  g[0] = w[0]; g[1] = w[1]; g[2] = w[2];
+}
+
 // Derivative shifts (src/libecp.c:240-248), indexed [order][shift].
 static __constant__ int c_shiftA[3][10] = {{0}, {+1, -1, 0, 0}, {+2, -2, +1, +1, -1, -1, 0, 0, +1, 0}};
 static __constant__ int c_shiftB[3][10] = {{0}, {0, 0, +1, -1}, {0, 0, +1, -1, +1, -1, +2, -2, 0, +1}};

@@ -137,19 +137,7 @@ __global__ void __launch_bounds__(128) k_shell_F(DevJob J) {
   const double *rC = J.geom + 3 * C, *rA = J.geom + 3 * A;
   double x = rC[0] - rA[0], y = rC[1] - rA[1], z = rC[2] - rA[2];
   const double dAC = sqrt(x * x + y * y + z * z);
-  if (threadIdx.x == 0) {
-    int end = J.gridEnd[c], j;
-    double R = J.radius[s], rmin = dAC - R, rmax = dAC + R;
-    for (j = end; j >= 0; j--)
-      if (J.xSmall[j] < rmin) break;
-    sw[0] = j + 1;
-    for (j = end; j >= 0; j--)
-      if (J.xSmall[j] <= rmax) break;
-    sw[1] = (j < 0 || J.xSmall[j] > rmax) ? -1 : j;
-    sw[2] = !(sw[1] >= sw[0]) || R < 0;
-    int *w = J.win + ((size_t)c * J.nShells + s) * 3;
-    w[0] = sw[0]; w[1] = sw[1]; w[2] = sw[2];
-  }
+  if (threadIdx.x == 0) shell_window(J, s, c, dAC, sw);
   __syncthreads();
   // run = derivative order of the table: rows up to L - 1 + l + run and
   // coefficients times zeta^run (src/type2.c:229, :263-290)
