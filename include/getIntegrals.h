@@ -13,6 +13,9 @@
  * Returns 0, or 1 if set-up failed (prints "error initializing libECP").  As
  * in the reference, quadrature failures are not reported here; use
  * ecpgb_getIntegrals (libecp_gb300.h) for a status.
+ * Engine: the plain FP64 kernels; the environment variable
+ * LIBECP_GB300_MODE=fast selects the batched FP64 engine (the same results
+ * within 1e-10, several times faster), =mixed the mixed-precision mode.
  */
 #ifndef GET_INTEGRALS_H
 #define GET_INTEGRALS_H 1

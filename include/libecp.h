@@ -14,7 +14,8 @@
  * integration error (src/libecp.h:23-27).  The reference then uses a freed
  * table and aborts in practice; here that quadrature keeps its full-grid
  * estimate and every block is still handed out.  -1: engine error (no GPU,
- * allocation).
+ * allocation).  LIBECP_GB300_MODE=fast in the environment runs the blocks on
+ * the batched FP64 engine (see getIntegrals.h).
  */
 #ifndef LIBECP_H
 #define LIBECP_H 1
