@@ -73,7 +73,7 @@ static __device__ void bessel_small(int lmax, double z, double *K, int stride) {
 
 template <bool kMixed>
 static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *K, int stride) {
-  if (z < 1.0E-7) {
+  if (__builtin_expect(z < 1.0E-7, 0)) {  // rare: laid out of line
     bessel_small(lmax, z, K, stride);
     return;
   }
@@ -128,7 +128,7 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
 
 // One row K_l(z), by the same branches as bessel_fast.
 static __device__ double bessel_row(const DevJob &J, int l, double z) {
-  if (z < 1.0E-7) {
+  if (__builtin_expect(z < 1.0E-7, 0)) {  // rare: laid out of line
     if (z <= 0) return l == 0 ? 1.0 : 0.0;
     double v = 1 - z;
     for (int i = 1; i <= l; i++) v = v * z / (2 * i + 1);
@@ -731,7 +731,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
               WR[l] = v;
             }
           }
-        } else if (n != nb && !upper && n < O && n >= ws && n < we) {
+        } else if (__builtin_expect(n != nb && !upper && n < O && n >= ws && n < we, 0)) {
           // beyond the break the reference integrates its small-grid buffers:
           // exponent and U_L at index n, r^l and K_l at flat offset l*OL + n of
           // rows written with the small grid's stride
@@ -840,7 +840,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
     const bool upper = t > 0 && ((t - 1) & 1);
     owner = -1;
     if (n < nb) owner = k;
-    else if (n != nb && !upper) {
+    else if (__builtin_expect(n != nb && !upper, 0)) {
       for (int j = k - 1; j >= 0; j--)
         if (S.ppBreak[j] >= n) { owner = j; break; }
       if (owner >= 0 && S.ppBreak[owner] == n) owner = -1;

@@ -61,7 +61,7 @@ ECPGB_HD double fast_exp(double x) {
   const double shifter = 0x1.8p52;
   // |x| < 708 (and not NaN): the result and 2^m are normal
   const bool common = (int)((unsigned long long)dbits(x) >> 32 & 0x7fffffffu) < 0x40862000;
-  if (!common) {
+  if (__builtin_expect(!common, 0)) {  // rare: |x| >= 708, NaN
     if (!(x > -745.2)) return (x != x) ? x : 0.0;  // NaN stays NaN, underflow to 0
     if (x > 709.78) return HUGE_VAL;
   }
