@@ -77,6 +77,29 @@ def test_fast_other_parameters(eg, order):
     assert_blocks_match(meta, data, mo, do)
 
 
+def test_fast_local_only_centre(eg):
+    """A centre with only a local channel (the reference aborts on it): the
+    type-1 part and a zero type-2 block, as the oracle."""
+    b = W._Builder()
+    b.atom([0.0, 0.0, 0.0], ecp=[(0, [(2.0, 2.0, 1.1)])], shells=[(1, [(0.7, 0.9)])])
+    b.atom([0.5, -0.3, 0.8], shells=[(0, [(0.5, 0.4), (0.3, 2.0)]), (2, [(1.0, 0.6)])])
+    s = b.build("local_only")
+    rc, mo, do = O.oracle_blocks(s)
+    meta, data = eg.blocks(s, mode=eg.ECPGB_FAST)
+    assert_blocks_match(meta, data, mo, do)
+
+
+def test_fast_empty_inputs(eg):
+    """No ECP centre: nothing is added, no block is emitted."""
+    b = W._Builder()
+    b.atom([0.0, 0.0, 0.0], shells=[(0, [(1.0, 1.0)])])
+    s = b.build("no ecp")
+    rc, I, _ = eg.get_integrals_info(s, mode=eg.ECPGB_FAST)
+    assert rc == 0 and np.all(I == 0.0)
+    meta, data = eg.blocks(s, mode=eg.ECPGB_FAST)
+    assert meta.shape == (0, 8)
+
+
 def test_fast_maximum_sizes(eg):
     rng = np.random.default_rng(5)
     b = W._Builder()
