@@ -5,7 +5,6 @@ integer and bit manipulation) is IEEE-defined, so the device build computes
 the same values."""
 import os
 import subprocess
-import tempfile
 
 import pytest
 
@@ -39,9 +38,8 @@ int main() {
 """
 
 
-def test_fast_exp_against_libm():
-    d = tempfile.mkdtemp()
-    src, exe = os.path.join(d, "t.cpp"), os.path.join(d, "t")
+def test_fast_exp_against_libm(tmp_path):
+    src, exe = str(tmp_path / "t.cpp"), str(tmp_path / "t")
     with open(src, "w") as f:
         f.write(SRC)
     inc = os.path.join(ROOT, "libecp_gb300", "csrc")
