@@ -1,6 +1,6 @@
 """fast_exp (libecp_gb300/csrc/ecp_fastmath.h) against the C library's exp.
 
-The header is compiled for the host here; every operation in it (fma, rint,
+The header is compiled for the host here; every operation in it (fma, add,
 integer and bit manipulation) is IEEE-defined, so the device build computes
 the same values."""
 import os
