@@ -11,13 +11,19 @@
 // loads the library and stays allocated until the process exits.
 //
 // Rules of use:
-//   * The first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before any stream capture on the device.
-//   * Every call shares the one array and overwrites it; calls that overlap on
-//     the GPU (two host threads, or a call racing another stream's kernels
-//     that read the array) race.  Calls from one thread run one after the
-//     other: each call synchronises the default stream before it returns.
+//   * Every call looks up the array's device address with
+//     cudaGetSymbolAddress on the current device (the lookup allocates
+//     nothing; looking it up each time keeps the address valid after a
+//     cudaDeviceReset reloads the module).  The first call on a device also
+//     loads the module there; make that first call before any stream capture
+//     on the device.
+//   * Every call shares the one array and overwrites it.  Inside the library
+//     the engine lock is held from the first write into the array to the
+//     final synchronisation, so two host threads calling this entry point do
+//     not interleave their jobs; but calls that overlap on the GPU with other
+//     work that reads or writes the array (a kernel of the caller's own that
+//     was handed the array, or a copy queued on another stream) race.  Each
+//     call synchronises the default stream before it returns.
 //   * Jobs whose buffers do not fit are rejected with an error naming the
 //     bytes needed; nothing is allocated to make them fit.
 //   * No CUDA allocation of any kind happens here (no cudaMalloc / cudaFree /
@@ -41,26 +47,20 @@ namespace ecpgb {
 constexpr size_t kScratchBytes = 64ull << 20;  // 64 MiB per device
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-static void *g_scratchPtr[kMaxDevices];  // device address of g_scratch, per device
-
-// Device address of the scratch array on the current device (looked up once).
+// Device address of the scratch array on the current device.
 static int scratch_address(void **out) {
   int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
     set_error("no usable CUDA device for the no-allocation entry point");
     return 1;
   }
-  if (!g_scratchPtr[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess || !p) {
-      set_error("cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
-      return 1;
-    }
-    g_scratchPtr[dev] = p;
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess || !p) {
+    set_error("cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
+    return 1;
   }
-  *out = g_scratchPtr[dev];
+  *out = p;
   return 0;
 }
 
@@ -88,14 +88,28 @@ int run_matrix_noalloc(const ecpgb_system &s, int rowdim, double *I) {
   if (rowdim < P.dim) { set_error("rowdim %d < basis dimension %d", rowdim, P.dim); return 1; }
   if (P.deriv) { set_error("the AO matrix exists for derivative order 0 only"); return 1; }
   if (P.nCentres == 0 || P.nPairs == 0) return 0;
-  void *sp = nullptr;
-  if (scratch_address(&sp)) return 1;
   HostTables h;
   build_tables(table_key(P), h);
   if (h.status) {
     set_error(h.status == 1 ? "Bessel series did not converge" : "table sizes out of range");
     return 1;
   }
+  // The level schedules live in __constant__ memory shared with the engine
+  // and with requests in flight on the server's streams: wait for those to
+  // finish (the wait releases the lock) and upload this job's schedules
+  // before the first write into the scratch array.  From here to the final
+  // synchronisation the lock stays held, so no other call of this entry
+  // point can rewrite the array under this job.
+  wait_schedules_unpinned(lk);
+  if (upload_schedules(h.s93.slot.data(), (int)h.s93.slot.size(), h.s93.lvEnd.data(), h.s93.lvJ.data(),
+                       h.s93.lvN.data(), h.s93.nLevels, h.s92.slot.data(), (int)h.s92.slot.size(),
+                       h.s92.lvEnd.data(), h.s92.lvN.data(), h.s92.nLevels, nullptr)) {
+    set_error("schedule upload failed");
+    return 1;
+  }
+  schedules_overwritten();
+  void *sp = nullptr;
+  if (scratch_address(&sp)) return 1;
   // used-triple lists per (la, lb, l), as the engine builds them
   const int LB = h.maxLBS, LE = h.maxLECP > 0 ? h.maxLECP : 1;
   std::vector<int> off, cnt, items, tmp;
@@ -193,16 +207,6 @@ int run_matrix_noalloc(const ecpgb_system &s, int rowdim, double *I) {
   J.p2s = p2s; J.fac = fac; J.dfac = dfac; J.omega = om; J.ijk = ijk; J.ijkIdx = ijkI;
   J.itemOff = iO; J.itemCnt = iC; J.items = iI;
 
-  // the level schedules live in __constant__ memory shared with the engine
-  // (and with requests in flight on the server's streams: wait for those)
-  wait_schedules_unpinned(lk);
-  if (upload_schedules(h.s93.slot.data(), (int)h.s93.slot.size(), h.s93.lvEnd.data(), h.s93.lvJ.data(),
-                       h.s93.lvN.data(), h.s93.nLevels, h.s92.slot.data(), (int)h.s92.slot.size(),
-                       h.s92.lvEnd.data(), h.s92.lvN.data(), h.s92.nLevels, nullptr)) {
-    set_error("schedule upload failed");
-    return 1;
-  }
-  schedules_overwritten();
   UnitSmem Lm = unit_smem_layout(h.maxLBS, h.maxLECP, h.nF);
   if (launch_fp64_pipeline(J, nullptr, sizeof(double) * (size_t)Lm.total, nullptr, nullptr)) {
     set_error("kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
