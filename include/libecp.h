@@ -37,9 +37,12 @@ typedef void (*ECPCallback)(int A, int sa, int la, int shifta,
 /* The reference's header names parameters 4 and 5 (KECP, lECP) but its
  * definition reads them as (lECP, KECP) (src/libecp.c:55), and getIntegrals
  * passes them in that order; this declaration follows the definition.
- * n: derivative order (0 only in this library -- other values return NULL).
- * lmax / shellOrdering: custom Cartesian ordering (NULL = libint default; a
- * custom ordering returns NULL in this library).
+ * n: nuclear-derivative order 0, 1 or 2, as the reference: blocks of the
+ * shells with l shifted by (shifta, shiftb) and coefficients times zeta^shift
+ * (src/libecp.c:240-374).
+ * lmax / shellOrdering: the caller's Cartesian ordering of shells 0..lmax
+ * (NULL = libint default), refused as the reference refuses it when lmax is
+ * too small (src/libecp.c:152-166).
  * Returns NULL on failure. */
 libECPHandle *libECP_init(int nrAtoms, double *geometry,
                           int *shellsECP, int *lECP, int *KECP,

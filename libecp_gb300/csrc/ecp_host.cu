@@ -245,6 +245,8 @@ static bool same_schedules(const DevTables *a, const DevTables *b) {
 struct Engine {
   std::mutex mu;
   cudaStream_t stream = nullptr;
+  // timing events of the one-shot runs (matrix, blocks), created once
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   // batched-path launch configuration per (maxLBS, maxLECP), set by the autotuner
   std::map<std::pair<int, int>, FastConfig> tuned;
   FastConfig config_for(int LB, int LE) const {
@@ -266,6 +268,7 @@ struct Engine {
       return -1;
     }
     CUDA_OK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    for (auto &e : ev) CUDA_OK(cudaEventCreate(&e));
     init = true;
     return 0;
   }
@@ -599,8 +602,7 @@ int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_inf
   JobBuffers &B = E.shared;
   DevJob J;
   if (stage_job(P, T, B, J, mode, E.stream)) return 1;
-  cudaEvent_t e0, e1, u0, u1;
-  cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
+  cudaEvent_t e0 = E.ev[0], e1 = E.ev[1], u0 = E.ev[2], u1 = E.ev[3];
   cudaEventRecord(e0, E.stream);
   if (run_pipeline(B, J, mode, u0, u1, nullptr, E.stream)) return 1;
   cudaEventRecord(e1, E.stream);
@@ -613,7 +615,6 @@ int run_matrix(const ecpgb_system &s, int mode, int rowdim, double *I, ecpgb_inf
   float ms = 0, msu = 0;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventElapsedTime(&msu, u0, u1);
-  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(u0); cudaEventDestroy(u1);
   const double *M = (const double *)B.pinnedOut.p;
   for (int i = 0; i < P.dim; i++)
     for (int j = i; j < P.dim; j++) I[(size_t)i * rowdim + j] += M[(size_t)i * P.dim + j];
@@ -653,8 +654,7 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
   if (stage_job(P, T, B, J, mode, E.stream)) return 1;
   const size_t nv = (size_t)P.nCentres * P.centreStride;
   cudaMemsetAsync(B.out.p, 0, sizeof(double) * nv, E.stream);
-  cudaEvent_t e0, e1, u0, u1;
-  cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&u0); cudaEventCreate(&u1);
+  cudaEvent_t e0 = E.ev[0], e1 = E.ev[1], u0 = E.ev[2], u1 = E.ev[3];
   cudaEventRecord(e0, E.stream);
   if (run_pipeline(B, J, mode, u0, u1, nullptr, E.stream)) return 1;
   cudaEventRecord(e1, E.stream);
@@ -667,7 +667,6 @@ int run_blocks(const ecpgb_system &s, int mode, double *values, long long *offse
   float ms = 0, msu = 0;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventElapsedTime(&msu, u0, u1);
-  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(u0); cudaEventDestroy(u1);
   long long emitted = 0;
   for (long long u = 0; u < nUnits; u++) {
     if (status) status[u] = st[u];

@@ -4,7 +4,7 @@
  * CPU restatement, in plain C and FP64, of chrr/libECP's ECP-integral path.
  * It is pinned against the reference itself: the committed fixtures under
  * tests/golden/ were produced by the unmodified reference (oracle/_ref, built
- * by oracle/Makefile) and tests/test_oracle_golden.py requires this file to
+ * by oracle/Makefile) and tests/test_oracle.py requires this file to
  * reproduce them.
  *
  * Structure (each part cites the reference code it restates):
