@@ -348,15 +348,45 @@ static void map_fm06(int n, const double *x0, const double *w0, double *x, doubl
 
 typedef double (*Integrand)(int idx, const void *ctx);
 
+/* Decisions taken within rounding noise.  The adaptive quadratures stop at
+ * the first level whose error test passes.  Where the test's two sides differ
+ * by less than a bound on their rounding error, any other correct FP64
+ * evaluation order (or a libm that differs by an ulp) can take the other
+ * branch, and the other branch can change the result by far more than an
+ * ulp: a small-grid quadrature that fails goes to the large-grid fallback,
+ * whose stale-buffer terms (see type2_fallback) the small grid never sees.
+ * With tracking on, such decisions are counted per block, and the blocks are
+ * recomputed with chosen decisions inverted; the parity tests accept a GPU
+ * block that matches the reference's branch or one of these alternatives.
+ * The bound on the rounding error of a quadrature's running sums is
+ * kappa * 2^-53 * (sum of |w f| over the points evaluated so far).  The
+ * primary results do not depend on any of this. */
+typedef struct {
+  int track;      /* count ambiguous decisions in this block */
+  int count;      /* ambiguous decisions met so far */
+  unsigned flip;  /* bit i: invert the i-th ambiguous decision */
+  double kappa;
+} Decisions;
+static __thread Decisions g_dec;
+
+static int decide(int pass, double lhs, double rhs, double noise) {
+  if (!g_dec.track || !(fabs(lhs - rhs) < noise)) return pass;
+  int i = g_dec.count++;
+  if (i < 32 && (g_dec.flip >> i & 1u)) return !pass;
+  return pass;
+}
+
 /* Adaptive PS93 walk (src/gc_integrators.c:157-217): absolute error test,
  * lower-half points counted only at or after `start`, upper-half points only
  * at or before `end`, levels that touch no point skip the test. */
 static int quad_ps93(const Sched *s, const double *w, int start, int end, double tol,
                      Integrand f, const void *ctx, double *res, OracleStats *st) {
   int order = s->order, n = 3;
+  double h1 = w[s->head[1]] * f(s->head[1], ctx), h2 = w[s->head[2]] * f(s->head[2], ctx);
   double p = w[s->head[0]] * f(s->head[0], ctx);
-  double q = w[s->head[1]] * f(s->head[1], ctx) + w[s->head[2]] * f(s->head[2], ctx);
+  double q = h1 + h2;
   double I = p + q, err = 0.0;
+  double sabs = fabs(p) + fabs(h1) + fabs(h2);
   long long pts = 3;
   st->ps93_calls++;
   for (int k = 0; k < s->nLevels; k++) {
@@ -365,8 +395,8 @@ static int quad_ps93(const Sched *s, const double *w, int start, int end, double
     for (int t = 0; t < s->lvCount[k]; t++) {
       int lo = lv[t], hi = order - lo - 1;
       double T = 0.0;
-      if (lo >= start) { T += w[lo] * f(lo, ctx); cnt++; }
-      if (hi <= end) { T += w[hi] * f(hi, ctx); cnt++; }
+      if (lo >= start) { double v = w[lo] * f(lo, ctx); T += v; sabs += fabs(v); cnt++; }
+      if (hi <= end) { double v = w[hi] * f(hi, ctx); T += v; sabs += fabs(v); cnt++; }
       I += T;
     }
     pts += cnt;
@@ -375,7 +405,9 @@ static int quad_ps93(const Sched *s, const double *w, int start, int end, double
     if (cnt > 0) err = 16 * fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q)) / (3 * n);
     q = (1 - j) * q + j * I;
     if (cnt == 0) continue;
-    if (err < tol) {
+    /* d combines three running sums: its rounding error is below 3 nu,
+       nu = kappa 2^-53 sabs, so err's is below 16 nu / n */
+    if (decide(err < tol, err, tol, 16.0 * g_dec.kappa * 0x1p-53 * sabs / n)) {
       *res = 16 * q / (3 * n);
       st->ps93_points += pts;
       return 0;
@@ -391,7 +423,7 @@ static int quad_ps93(const Sched *s, const double *w, int start, int end, double
 static int quad_psm92(const Sched *s, const double *w, int start, int end, double tol,
                       Integrand f, const void *ctx, double *res, OracleStats *st) {
   int order = s->order, M = s->head[0];
-  double I = w[M] * f(M, ctx), p = I, q, e, N;
+  double I = w[M] * f(M, ctx), p = I, q, e, N, sabs = fabs(I);
   long long pts = 1;
   st->psm92_calls++;
   for (int k = 0; k < s->nLevels; k++) {
@@ -402,15 +434,18 @@ static int quad_psm92(const Sched *s, const double *w, int start, int end, doubl
     for (int t = 0; t < s->lvCount[k]; t++) {
       int lo = lv[t], hi = order - lo - 1;
       double T = 0.0;
-      if (lo >= start) { T += w[lo] * f(lo, ctx); cnt++; }
-      if (hi <= end) { T += w[hi] * f(hi, ctx); cnt++; }
+      if (lo >= start) { double v = w[lo] * f(lo, ctx); T += v; sabs += fabs(v); cnt++; }
+      if (hi <= end) { double v = w[hi] * f(hi, ctx); T += v; sabs += fabs(v); cnt++; }
       I += T;
     }
     pts += cnt;
     N = s->lvN[k] + 1.0;
     e = I - p;
     if (cnt == 0) continue;
-    if (16 * e * e <= 3 * N * fabs(I - q) * tol) {
+    /* e, I - q: rounding error below 4 nu each (p, q are doubled sums) */
+    const double nu = g_dec.kappa * 0x1p-53 * sabs;
+    const double lhs = 16 * e * e, rhs = 3 * N * fabs(I - q) * tol;
+    if (decide(lhs <= rhs, lhs, rhs, 16 * (8 * fabs(e) * nu + 16 * nu * nu) + 3 * N * tol * 4 * nu)) {
       *res = 16 * I / (3 * N);
       st->psm92_points += pts;
       return 0;
@@ -1319,7 +1354,7 @@ static void poly_shift(const Sys *S, const double *gam, int la, const double *us
 
 /* ------------------------------------------------------------- the driver */
 
-typedef struct {
+typedef struct Sink {
   /* getIntegrals-style accumulation */
   double *I;
   int rowdim;
@@ -1329,6 +1364,7 @@ typedef struct {
   long long maxData, nData;
   double *data;
   int overflow;
+  struct Sink *alt; /* blocks with ambiguous decisions inverted, or NULL */
 } Sink;
 
 static void emit(const Sys *S, Sink *k, int C, int sa, int sb, int type, const double *blk) {
@@ -1376,14 +1412,42 @@ static int run_centre(const Sys *S, int C, const double *radius, Sink *k, Oracle
           st->blocks++;
           /* a large-grid quadrature that runs out of levels keeps its
              full-grid estimate (counted in stats->psm92_failed) */
-          memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
-          type1_block(S, &cc, sa, sb, ws, we, chi, st);
-          poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm1, blk, st);
-          emit(S, k, C, sa, sb, 1, blk);
-          memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
-          type2_block(S, &cc, sa, sb, ws, we, chi, st);
-          poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm2, blk, st);
-          emit(S, k, C, sa, sb, 2, blk);
+          for (int type = 1; type <= 2; type++) {
+            const double norm = type == 1 ? norm1 : norm2;
+            g_dec.track = k->alt != NULL;
+            g_dec.count = 0;
+            g_dec.flip = 0;
+            memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
+            if (type == 1) type1_block(S, &cc, sa, sb, ws, we, chi, st);
+            else type2_block(S, &cc, sa, sb, ws, we, chi, st);
+            poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm, blk, st);
+            emit(S, k, C, sa, sb, type, blk);
+            const int m = g_dec.count;
+            if (!k->alt || m == 0) continue;
+            /* alternatives: every non-empty subset of the ambiguous
+               decisions when there are at most 4, else each one alone and
+               all of them together */
+            unsigned masks[20];
+            int nm = 0;
+            if (m <= 4) {
+              for (unsigned v = 1; v < (1u << m); v++) masks[nm++] = v;
+            } else {
+              for (int i = 0; i < 18 && i < m; i++) masks[nm++] = 1u << i;
+              masks[nm++] = m >= 32 ? ~0u : (1u << m) - 1u;
+            }
+            OracleStats scratch;
+            for (int v = 0; v < nm; v++) {
+              memset(&scratch, 0, sizeof scratch);
+              g_dec.count = 0;
+              g_dec.flip = masks[v];
+              memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
+              if (type == 1) type1_block(S, &cc, sa, sb, ws, we, chi, &scratch);
+              else type2_block(S, &cc, sa, sb, ws, we, chi, &scratch);
+              poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm, blk, &scratch);
+              emit(S, k->alt, C, sa, sb, type, blk);
+            }
+          }
+          g_dec.track = 0;
         }
   free(chi);
   free(blk);
@@ -1452,6 +1516,27 @@ int oracle_blocks(SYS_ARGS, int centerLo, int centerHi, int maxBlocks, int *meta
   *nBlocks = k.nBlocks;
   *nData = k.nData;
   if (k.overflow) return -2;
+  return st;
+}
+
+int oracle_blocks_alt(SYS_ARGS, int centerLo, int centerHi, double kappa, int maxBlocks,
+                      int *meta, long long maxData, double *data, int *nBlocks,
+                      long long *nData, int maxAlt, int *altMeta, long long maxAltData,
+                      double *altData, int *nAlt, long long *nAltData, OracleStats *stats) {
+  Sink k, a;
+  memset(&k, 0, sizeof k);
+  memset(&a, 0, sizeof a);
+  k.maxBlocks = maxBlocks; k.meta = meta; k.maxData = maxData; k.data = data;
+  a.maxBlocks = maxAlt; a.meta = altMeta; a.maxData = maxAltData; a.data = altData;
+  k.alt = &a;
+  g_dec.kappa = kappa;
+  int st = run(SYS_PASS, centerLo, centerHi, NULL, &k, stats);
+  g_dec.kappa = 0.0;
+  *nBlocks = k.nBlocks;
+  *nData = k.nData;
+  *nAlt = a.nBlocks;
+  *nAltData = a.nData;
+  if (k.overflow || a.overflow) return -2;
   return st;
 }
 

@@ -77,6 +77,22 @@ int oracle_blocks(int nrAtoms, const double *geometry,
 /* getIntegrals over nThreads POSIX threads: ECP centres are dealt round-robin
  * to threads, each thread owns a private matrix, and the partial matrices are
  * summed into I at the end.  Used as the all-core CPU baseline. */
+/* As oracle_blocks, plus alternative blocks: for every block whose
+ * quadratures took a convergence decision within rounding noise (the test's
+ * two sides closer than kappa * 2^-53 * sum |w f| allows), the block
+ * recomputed with chosen such decisions inverted, recorded with the same
+ * meta rows into altMeta / altData (several per block possible). */
+int oracle_blocks_alt(int nrAtoms, const double *geometry,
+                      const int *shellsECP, const int *KECP, const int *lECP,
+                      const double *nECP, const double *dECP, const double *aECP,
+                      const int *shellsBS, const int *lBS, const int *KBS,
+                      const double *dBS, const double *aBS,
+                      int largeGridOrder, double tolerance, double accuracy,
+                      int centerLo, int centerHi, double kappa, int maxBlocks, int *meta,
+                      long long maxData, double *data, int *nBlocks, long long *nData,
+                      int maxAlt, int *altMeta, long long maxAltData, double *altData,
+                      int *nAlt, long long *nAltData, OracleStats *stats);
+
 int oracle_getIntegrals_mt(int nrAtoms, const double *geometry,
                            const int *shellsECP, const int *KECP, const int *lECP,
                            const double *nECP, const double *dECP, const double *aECP,

@@ -109,3 +109,37 @@ def test_grids_integrate(which, npts, order):
     else:
         val, ref = 16 * np.sum(w / (1 + x ** 2)) / (3 * (m + 1)), math.pi / 2
     assert abs(val - ref) < 1e-12
+
+
+def test_alternatives_leave_the_reference_branch_unchanged():
+    """With decision tracking on, the primary blocks are exactly the
+    oracle's; alternatives exist only for blocks whose quadratures took a
+    decision within the noise bound, and the bound grows with kappa."""
+    s = W.random_system(16, n_atoms=4, n_centres=2, lmax_basis=3, lmax_ecp=4, kmax=4,
+                        elo=0.01, ehi=500.0)
+    rc, m0, d0 = O.oracle_blocks(s)
+    counts = []
+    for kappa in (0.0, 16.0, 1e6):
+        rc2, m, d, am, ad = O.oracle_blocks_alt(s, kappa)
+        assert rc2 == rc and np.array_equal(m, m0) and np.array_equal(d, d0)
+        counts.append(len(am))
+        keys = {tuple(r) for r in m.tolist()}
+        assert all(tuple(r) in keys for r in am.tolist())
+    assert counts[0] == 0 and counts[0] <= counts[1] <= counts[2] and counts[2] > 0
+    # the matcher: a block equal to an alternative passes, a perturbed one does not
+    rc2, m, d, am, ad = O.oracle_blocks_alt(s, 1e6)
+    n0 = ((am[0][2] + 1) * (am[0][2] + 2) // 2) * ((am[0][5] + 1) * (am[0][5] + 2) // 2)
+    off = 0
+    for row in m:
+        n = ((row[2] + 1) * (row[2] + 2) // 2) * ((row[5] + 1) * (row[5] + 2) // 2)
+        if np.array_equal(row, am[0]):
+            break
+        off += n
+    g = d.copy()
+    g[off:off + n0] = ad[:n0]
+    bar = lambda r: 1e-10 + 1e-13 * float(np.max(np.abs(r)))
+    res = O.match_blocks(m, g, m, d, am, ad, bar)
+    assert not res["failures"]
+    g[off] += 1.0
+    res = O.match_blocks(m, g, m, d, am, ad, bar)
+    assert len(res["failures"]) == 1
