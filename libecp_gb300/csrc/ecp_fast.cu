@@ -203,6 +203,59 @@ static __device__ double channel(const DevJob &J, int c, int l, double r) {
   }
 }
 
+// Small-grid prefactor of a type-1 primitive pair, C1 = ca cb exp(zd2) with
+// zd2 = -za dAC^2 - zb dBC^2 (src/type1.c:235-246), rounded as the reference
+// rounds it (no contraction), so that every evaluation of it agrees.
+static __device__ inline double t1_prefactor(double za, double ca, double zb, double cb, double dAC, double dBC) {
+  const double zd2 = __dsub_rn(__dmul_rn(__dmul_rn(-za, dAC), dAC), __dmul_rn(__dmul_rn(zb, dBC), dBC));
+  return __dmul_rn(__dmul_rn(ca, cb), fast_exp(zd2));
+}
+
+// Kinds of type-1 primitive pairs.  The reference's small-grid integrand is
+// C1 r^l U K exp(e), e = (z r + s) r, multiplied left to right
+// (src/type1.c:79-88).
+//  * normal: C1 >= 2^-900 and e <= s^2 / (4 (za + zb)) < 700: no partial
+//    product of a non-negligible term underflows and exp(e) cannot overflow,
+//    so the integrand can be regrouped (prefactor, weight and r^l in one
+//    table row);
+//  * band: C1 below 2^-900 but not 0, or exp(e) may overflow: partial
+//    products underflow (or overflow) where a regrouped product would not, so
+//    the integrand is evaluated in the reference's order;
+//  * zero: C1 = 0, so every integrand value is 0 * (finite) = 0, or NaN where
+//    exp(e) overflows -- no table is needed.
+constexpr int kPairNormal = 0, kPairBand = 1, kPairZero = 2;
+constexpr double kLnDblMax = 0x1.62e42fefa39efp+9;  // exp overflows above it
+
+// e = (z r + s) r as the reference rounds it.
+static __device__ inline double t1_exponent(double z, double s, double r) {
+  return __dmul_rn(__dadd_rn(__dmul_rn(z, r), s), r);
+}
+
+// A zero-kind pair's PS93 walk (src/gc_integrators.c:157-217) with an
+// integrand that is 0 except NaN at window points whose exp(e) overflows:
+// the first level that counts a point converges to 0 unless a NaN has been
+// summed by then, after which no level converges.
+static __device__ bool t1_zero_walk(const DevJob &J, double s, double z, int ws, int we) {
+  auto nan_at = [&](int n) {
+    if (n < ws || n >= we) return false;
+    const double e = t1_exponent(z, s, J.xSmall[n]);
+    return e >= J.lnAcc1 && e > kLnDblMax;
+  };
+  bool nan = nan_at(c93_slot[0]) || nan_at(c93_slot[1]) || nan_at(c93_slot[2]);
+  int pos = 3;
+  for (int k = 0; k < c93_nLevels; k++) {
+    const int e = c93_lvEnd[k];
+    int cnt = 0;
+    for (; pos < e; pos += 2) {
+      const int lo = c93_slot[pos], hi = c93_slot[pos + 1];
+      if (lo >= ws) { nan = nan || nan_at(lo); cnt++; }
+      if (hi <= we) { nan = nan || nan_at(hi); cnt++; }
+    }
+    if (cnt > 0) return !nan;
+  }
+  return false;
+}
+
 // FM06 map parameters (src/gc_integrators.c:317-331).
 static __device__ inline void fm06(double za, double zb, double dAC, double dBC, double &i1, double &i2) {
   double zp = za + zb, P = (za * dAC + zb * dBC) / zp;
@@ -424,7 +477,10 @@ size_t fast_smem_bytes(int LB, int LE, int cap, int maxNP) {
 }
 
 struct FastShared {
+  // type-2 fallback: break index per primitive pair; during type 1 the
+  // primitive pairs ordered by kind (normal, band, zero)
   int ppBreak[kMaxContraction * kMaxContraction];
+  int t1Count[3];
   int failIdx[kWalkCap];
   unsigned failMask[64];
   int nFail, nThis, nextBase;
@@ -528,9 +584,9 @@ static __device__ void rsh_column(const DevJob &J, int lmax, int m, double x, do
 // A group of G primitive pairs (p0 .. p0+G-1) of the type-1 block, by one
 // warp (src/type1.c:95-302); lane = (pair, quadrature).  Adds the group's terms
 // to the warp's per-combined-index accumulators H.
-template <bool kMixed>
+template <bool kMixed, int kKind>
 static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *W, int c, int Lc,
-                                    int la, int lb, int p0, int G, int Nb, const double *pzA,
+                                    int la, int lb, const int *perm, int p0, int G, int Nb, const double *pzA,
                                     const double *pcA, const double *pzB, const double *pcB,
                                     const double *gA, const double *gB, int ws, int we, int pa0, int pb0,
                                     int &warn) {
@@ -543,7 +599,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
   const double *uL = J.uL + (size_t)c * O;
   // (1) per pair: k-vector, its spherical coordinates, the prefactor
   if (lane < G) {
-    int k = p0 + lane;
+    int k = perm[p0 + lane];
     // derivative blocks: coefficients times zeta^max(0, shift) (src/type1.c:239-246)
     double za = pzA[k / Nb], ca = zeta_times(pcA[k / Nb], za, pa0), zb = pzB[k % Nb],
            cb = zeta_times(pcB[k % Nb], zb, pb0);
@@ -551,7 +607,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * gA[i] + zb * gB[i]);
     sc[lane * 6 + 0] = sqrt(P[0] * P[0] + P[1] * P[1] + P[2] * P[2]);  // |P|, as src/util.c:75-106
     direction(P, sc[lane * 6 + 1], sc[lane * 6 + 2], sc[lane * 6 + 5]);
-    sc[lane * 6 + 3] = ca * cb * fast_exp(-za * dAC * dAC - zb * dBC * dBC);
+    sc[lane * 6 + 3] = t1_prefactor(za, ca, zb, cb, dAC, dBC);
     sc[lane * 6 + 4] = -za - zb;
   }
   __syncwarp();
@@ -574,6 +630,10 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
   double I = 0, p = 0, q = 0;
   bool done = !mine;
   int k = 0, cnt = 0;
+  if constexpr (kKind == kPairZero) {
+    // converged quadratures add 0 to Q; failed ones go to the fallback
+    if (mine) done = t1_zero_walk(J, sc[g * 6], sc[g * 6 + 4], ws, we);
+  } else
   for (int s0 = 0; s0 < O;) {
     const int s1 = step_end93(s0) < O ? step_end93(s0) : O;
     // slot entry: [0, lq) K_l(s r), [lq, 2lq) w * C1 U_L e^(..) r^l; zero
@@ -607,30 +667,53 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       const int gg = live_pair(e % nLive), t = __ldg(J.byN93 + s0 + lo + e / nLive), n = __ldg(J.s93 + t);
       double *ent = tab + ((t - s0) * G + gg) * TSs;
       const double s = sc[gg * 6];
-      double r = J.xSmall[n], ex = (sc[gg * 6 + 4] * r + s) * r;
-      ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
-      const double wB = J.wSmall[n] * (sc[gg * 6 + 3] * uL[n] * ex);
-      bessel_fast<kMixed>(J, lab, s * r, ent, 1);
-      double *WR = ent + lq, v = wB;
-      WR[0] = v;
-      for (int l = 1; l <= lab; l++) {
-        v *= r;
-        WR[l] = v;
+      double *WR = ent + lq;
+      if constexpr (kKind == kPairBand) {
+        // row l: (C1 r^l) U; the walk multiplies by K, exp(e) and w in turn
+        const double r = J.xSmall[n], e = t1_exponent(sc[gg * 6 + 4], s, r), C1 = sc[gg * 6 + 3];
+        bessel_fast<kMixed>(J, lab, s * r, ent, 1);
+        double R = 1.0;
+        for (int l = 0; l <= lab; l++) {
+          if (l) R = __dmul_rn(r, R);
+          WR[l] = __dmul_rn(__dmul_rn(C1, R), uL[n]);
+        }
+        ent[2 * lq] = e >= J.lnAcc1 ? fast_exp(e) : 0.0;
+      } else {
+        double r = J.xSmall[n], ex = (sc[gg * 6 + 4] * r + s) * r;
+        ex = ex >= J.lnAcc1 ? fast_exp(ex) : 0.0;
+        const double wB = J.wSmall[n] * (sc[gg * 6 + 3] * uL[n] * ex);
+        bessel_fast<kMixed>(J, lab, s * r, ent, 1);
+        double v = wB;
+        WR[0] = v;
+        for (int l = 1; l <= lab; l++) {
+          v *= r;
+          WR[l] = v;
+        }
       }
     }
     for (int e = lane; e < (ns - nIn) * nLive; e += 32) {
       const int i = e / nLive, t = __ldg(J.byN93 + s0 + (i < lo ? i : i + nIn));
       double *ent = tab + ((t - s0) * G + live_pair(e % nLive)) * TSs;
-      for (int l = 0; l < 2 * lq; l++) ent[l] = 0.0;
+      for (int l = 0; l <= 2 * lq; l++) ent[l] = 0.0;
     }
     __syncwarp();
     auto ent_of = [&](int t) { return tab + ((t - s0) * G + g) * TSs; };
+    // band kind: w * ((((C1 r^l1) U) K_l2) exp(e)), each product rounded
+    auto wf = [&](int t, int n) {
+      const double *e = ent_of(t);
+      return __dmul_rn(J.wSmall[n], __dmul_rn(__dmul_rn(e[lq + l1], e[l2]), e[2 * lq]));
+    };
     int t = s0;
     if (t == 0) {
       if (!done) {
-        const double *e0 = ent_of(0), *e1 = ent_of(1), *e2 = ent_of(2);
-        p = e0[lq + l1] * e0[l2];
-        q = fma(e2[lq + l1], e2[l2], e1[lq + l1] * e1[l2]);
+        if constexpr (kKind == kPairBand) {
+          p = wf(0, c93_slot[0]);
+          q = __dadd_rn(wf(1, c93_slot[1]), wf(2, c93_slot[2]));
+        } else {
+          const double *e0 = ent_of(0), *e1 = ent_of(1), *e2 = ent_of(2);
+          p = e0[lq + l1] * e0[l2];
+          q = fma(e2[lq + l1], e2[l2], e1[lq + l1] * e1[l2]);
+        }
         I = p + q;
       }
       t = 3;
@@ -640,8 +723,13 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       if (t == lvStart) cnt = 0;
       int lo = c93_slot[t], hi = c93_slot[t + 1];
       double T = 0.0;
-      if (lo >= ws) { if (!done) { const double *e = ent_of(t); T = e[lq + l1] * e[l2]; } cnt++; }
-      if (hi <= we) { if (!done) { const double *e = ent_of(t + 1); T = fma(e[lq + l1], e[l2], T); } cnt++; }
+      if constexpr (kKind == kPairBand) {
+        if (lo >= ws) { if (!done) T = wf(t, lo); cnt++; }
+        if (hi <= we) { if (!done) T = __dadd_rn(T, wf(t + 1, hi)); cnt++; }
+      } else {
+        if (lo >= ws) { if (!done) { const double *e = ent_of(t); T = e[lq + l1] * e[l2]; } cnt++; }
+        if (hi <= we) { if (!done) { const double *e = ent_of(t + 1); T = fma(e[lq + l1], e[l2], T); } cnt++; }
+      }
       if (!done) I += T;
       t += 2;
       if (t == c93_lvEnd[k]) {
@@ -671,7 +759,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
   for (int gg = 0; gg < G; gg++) {
     const bool fail = failed && g == gg;
     if (!__ballot_sync(0xffffffffu, fail)) continue;
-    const int kk = p0 + gg;
+    const int kk = perm[p0 + gg];
     const double za = pzA[kk / Nb], ca = zeta_times(pcA[kk / Nb], za, pa0), zb = pzB[kk % Nb],
                  cb = zeta_times(pcB[kk % Nb], zb, pb0);
     const double s = sc[gg * 6], z = -za - zb, zd2 = -za * dAC * dAC - zb * dBC * dBC;
@@ -1066,15 +1154,76 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     const int ncab = (lab + 1) * (lab + 2) * (lab + 3) / 6;
     for (int e = tid & 31; e < ncab; e += 32) W[Lm.w1H + e] = 0.0;
     __syncwarp();
-    int G = t1_group(lab, J.gcap);
-    // balance: with few primitive pairs, narrower groups keep all warps busy
-    if (J.balance) {
-      const int Gb = (NP + kWarps - 1) / kWarps;
-      if (Gb < G) G = Gb > 0 ? Gb : 1;
+    // primitive pairs by kind (normal, band, zero), each kind in pair order
+    int *perm = S.ppBreak;
+    if (warp == 0) {
+      const int lane = tid & 31;
+      int base[3] = {0, 0, 0};
+      for (int k0 = 0; k0 < NP; k0 += 32) {
+        const int k = k0 + lane;
+        int kind = -1;
+        if (k < NP) {
+          const double za = pzA[k / Nb], ca = zeta_times(pcA[k / Nb], za, pa0), zb = pzB[k % Nb],
+                       cb = zeta_times(pcB[k % Nb], zb, pb0);
+          const double C1 = t1_prefactor(za, ca, zb, cb, dAC, dBC);
+          double P[3];
+          for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * gA[i] + zb * gB[i]);
+          const double s2 = P[0] * P[0] + P[1] * P[1] + P[2] * P[2];
+          kind = C1 == 0.0 ? kPairZero : (C1 < 0x1p-900 || s2 > 2800.0 * (za + zb)) ? kPairBand : kPairNormal;
+        }
+        // first pass: counts only
+        for (int kd = 0; kd < 3; kd++) base[kd] += __popc(__ballot_sync(0xffffffffu, kind == kd));
+      }
+      if (lane == 0) { S.t1Count[0] = base[0]; S.t1Count[1] = base[1]; S.t1Count[2] = base[2]; }
+      int pos[3] = {0, base[0], base[0] + base[1]};
+      for (int k0 = 0; k0 < NP; k0 += 32) {
+        const int k = k0 + lane;
+        int kind = -1;
+        if (k < NP) {
+          const double za = pzA[k / Nb], ca = zeta_times(pcA[k / Nb], za, pa0), zb = pzB[k % Nb],
+                       cb = zeta_times(pcB[k % Nb], zb, pb0);
+          const double C1 = t1_prefactor(za, ca, zb, cb, dAC, dBC);
+          double P[3];
+          for (int i = 0; i < 3; i++) P[i] = 2.0 * (za * gA[i] + zb * gB[i]);
+          const double s2 = P[0] * P[0] + P[1] * P[1] + P[2] * P[2];
+          kind = C1 == 0.0 ? kPairZero : (C1 < 0x1p-900 || s2 > 2800.0 * (za + zb)) ? kPairBand : kPairNormal;
+        }
+        for (int kd = 0; kd < 3; kd++) {
+          const unsigned m = __ballot_sync(0xffffffffu, kind == kd);
+          if (kind == kd) perm[pos[kd] + __popc(m & ((1u << lane) - 1u))] = k;
+          pos[kd] += __popc(m);
+        }
+      }
     }
-    for (int p0 = warp * G; p0 < NP; p0 += kWarps * G)
-      t1_group_run<kMixed>(J, Lm, W, c, Lc, la, lb, p0, NP - p0 < G ? NP - p0 : G, Nb, pzA, pcA, pzB, pcB, gA, gB,
-                   ws, we, pa0, pb0, warn1);
+    __syncthreads();
+    // groups of each kind, dealt to the warps round-robin over all kinds
+    int Gk[3], nG[3], nGroups = 0;
+    for (int kd = 0; kd < 3; kd++) {
+      const int n = S.t1Count[kd];
+      int G = t1_group(lab, J.gcap);
+      // balance: with few primitive pairs, narrower groups keep all warps busy
+      if (J.balance) {
+        const int Gb = (n + kWarps - 1) / kWarps;
+        if (Gb < G) G = Gb > 0 ? Gb : 1;
+      }
+      Gk[kd] = G;
+      nG[kd] = (n + G - 1) / G;
+      nGroups += nG[kd];
+    }
+    for (int gi = warp; gi < nGroups; gi += kWarps) {
+      int kd = 0, gj = gi, off = 0;
+      while (gj >= nG[kd]) { gj -= nG[kd]; off += S.t1Count[kd]; kd++; }
+      const int p0 = off + gj * Gk[kd], n = S.t1Count[kd] - gj * Gk[kd], G = n < Gk[kd] ? n : Gk[kd];
+      if (kd == kPairNormal)
+        t1_group_run<kMixed, kPairNormal>(J, Lm, W, c, Lc, la, lb, perm, p0, G, Nb, pzA, pcA, pzB, pcB, gA, gB,
+                                          ws, we, pa0, pb0, warn1);
+      else if (kd == kPairBand)
+        t1_group_run<kMixed, kPairBand>(J, Lm, W, c, Lc, la, lb, perm, p0, G, Nb, pzA, pcA, pzB, pcB, gA, gB,
+                                        ws, we, pa0, pb0, warn1);
+      else
+        t1_group_run<kMixed, kPairZero>(J, Lm, W, c, Lc, la, lb, perm, p0, G, Nb, pzA, pcA, pzB, pcB, gA, gB,
+                                        ws, we, pa0, pb0, warn1);
+    }
     // the type-2 small-grid quadratures, 32 at a time to whichever warp is
     // through with its type-1 groups (each writes its own entry of T: the
     // result does not depend on the warp)

@@ -63,7 +63,9 @@ ECPGB_HD double fast_exp(double x) {
   const bool common = (int)((unsigned long long)dbits(x) >> 32 & 0x7fffffffu) < 0x40862000;
   if (__builtin_expect(!common, 0)) {  // rare: |x| >= 708, NaN
     if (!(x > -745.2)) return (x != x) ? x : 0.0;  // NaN stays NaN, underflow to 0
-    if (x > 709.78) return HUGE_VAL;
+    // overflow exactly where exp overflows: above ln(DBL_MAX) rounded to
+    // the nearest double (a result of 0 * exp(x) is 0 below it, NaN above)
+    if (x > 0x1.62e42fefa39efp+9) return HUGE_VAL;
   }
   const double t = std::fma(x, ECPGB_EXP2_INV, shifter);
   const int n = (int)dbits(t);  // low word of t: the nearest integer to x * 512 / ln2
@@ -85,6 +87,7 @@ ECPGB_HD double fast_exp(double x) {
     return std::fma(sm, p, sm);
   }
   const double y = std::fma(s, p, s);
+  if (m > 1023) return (y * pow2i(m - 1)) * 2.0;  // just below the overflow threshold
   if (m >= -1020) return y * pow2i(m);
   return (y * pow2i(m + 54)) * 0x1p-54;  // result subnormal: scale in two steps
 }

@@ -369,6 +369,12 @@ typedef struct {
 } Decisions;
 static __thread Decisions g_dec;
 
+/* With g_abs set, the angular contractions of a block also accumulate the
+ * absolute values of their terms there (same indices as the block's chi), so
+ * that poly_shift_abs gives each element's sum of |terms|: the scale of the
+ * rounding error any correct FP64 evaluation of the block carries. */
+static __thread double *g_abs;
+
 static int decide(int pass, double lhs, double rhs, double noise) {
   if (!g_dec.track || !(fabs(lhs - rhs) < noise)) return pass;
   int i = g_dec.count++;
@@ -1142,6 +1148,7 @@ static int type1_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, i
                     for (int m = 0; m < 2 * l + 1; m++)
                       factor += rsh[LM(l, m)] * S->p2s[(size_t)p * tmW + LM(l, m)];
                     chi[i * inc + j] += factor * Q[lmax * (lab + 1) + l];
+                    if (g_abs) g_abs[i * inc + j] += fabs(factor * Q[lmax * (lab + 1) + l]);
                     st->contraction_fma += 2 * l + 2;
                   }
                 }
@@ -1285,16 +1292,18 @@ static int type2_block(const Sys *S, const Centre *cc, int sa, int sb, int ws, i
           ll2 = par2 > ll2 ? par2 : ll2;
           for (int c2 = 0; c2 < NCART(beta); c2++) {
             int q = NCUM(beta - 1) + c2;
-            double tmp = 0.0;
+            double tmp = 0.0, tabs = 0.0;
             for (int l1 = ll1; l1 <= la + l; l1 += 2)
               for (int l2 = ll2; l2 <= lb + l; l2 += 2) {
                 double factor = 0.0;
                 for (int m = 0; m < 2 * l + 1; m++)
                   factor += omA[l1 * aI2 + LM(l, m) * aI1 + p] * omB[l2 * bI2 + LM(l, m) * bI1 + q];
                 tmp += factor * T[(l1 * n2 + l2) * n3 + ab];
+                tabs += fabs(factor * T[(l1 * n2 + l2) * n3 + ab]);
                 st->contraction_fma += 2 * l + 2;
               }
             gam[p * inc + q] += tmp;
+            if (g_abs) g_abs[p * inc + q] += tabs;
           }
         }
       }
@@ -1352,6 +1361,44 @@ static void poly_shift(const Sys *S, const double *gam, int la, const double *us
   free(J);
 }
 
+/* poly_shift over absolute values: the largest element of the result. */
+static double poly_shift_abs(const Sys *S, const double *gam, int la, const double *uspA, int dA, int lb,
+                             const double *uspB, int dB, double norm) {
+  int d = S->ijkDim, incG = NCUM(lb), incJ = NCUM(lb), incI = NCART(lb);
+  const double *fac = S->fac;
+  double *J = calloc((size_t)NCART(la) * NCUM(lb), sizeof(double));
+  double *out = calloc((size_t)NCART(la) * NCART(lb), sizeof(double));
+  for (int c1 = 0; c1 < NCART(la); c1++) {
+    const int *e = S->ijk + 3 * (NCUM(la - 1) + c1);
+    for (int x = 0; x <= e[0]; x++)
+      for (int y = 0; y <= e[1]; y++)
+        for (int z = 0; z <= e[2]; z++) {
+          double f = binom(e[0], x, fac) * binom(e[1], y, fac) * binom(e[2], z, fac) *
+                     uspA[((e[0] - x) * dA + (e[1] - y)) * dA + (e[2] - z)];
+          if (fabs(f) <= S->acc) continue;
+          int r = S->ijkIdx[(x * d + y) * d + z];
+          for (int q = 0; q < NCUM(lb); q++) J[c1 * incJ + q] += fabs(f) * gam[r * incG + q];
+        }
+  }
+  double mx = 0.0;
+  for (int c2 = 0; c2 < NCART(lb); c2++) {
+    const int *e = S->ijk + 3 * (NCUM(lb - 1) + c2);
+    for (int x = 0; x <= e[0]; x++)
+      for (int y = 0; y <= e[1]; y++)
+        for (int z = 0; z <= e[2]; z++) {
+          double f = binom(e[0], x, fac) * binom(e[1], y, fac) * binom(e[2], z, fac) *
+                     uspB[((e[0] - x) * dB + (e[1] - y)) * dB + (e[2] - z)];
+          if (fabs(f) <= S->acc) continue;
+          int r = S->ijkIdx[(x * d + y) * d + z];
+          for (int c1 = 0; c1 < NCART(la); c1++) out[c1 * incI + c2] += fabs(f * norm) * J[c1 * incJ + r];
+        }
+  }
+  for (int i = 0; i < NCART(la) * NCART(lb); i++) mx = out[i] > mx ? out[i] : mx;
+  free(J);
+  free(out);
+  return mx;
+}
+
 /* ------------------------------------------------------------- the driver */
 
 typedef struct Sink {
@@ -1365,6 +1412,7 @@ typedef struct Sink {
   double *data;
   int overflow;
   struct Sink *alt; /* blocks with ambiguous decisions inverted, or NULL */
+  double *scale;    /* per recorded block: largest sum of |terms| of an element, or NULL */
 } Sink;
 
 static void emit(const Sys *S, Sink *k, int C, int sa, int sb, int type, const double *blk) {
@@ -1395,6 +1443,7 @@ static int run_centre(const Sys *S, int C, const double *radius, Sink *k, Oracle
   centre_build(S, C, &cc, radius, st);
   int lmaxBS = S->maxLBS;
   double *chi = malloc(sizeof(double) * NCUM(lmaxBS) * NCUM(lmaxBS));
+  double *chiAbs = malloc(sizeof(double) * NCUM(lmaxBS) * NCUM(lmaxBS));
   double *blk = malloc(sizeof(double) * NCART(lmaxBS) * NCART(lmaxBS));
   int status = 0;
   for (int A = 0; A < S->nAtoms && !status; A++)
@@ -1418,9 +1467,14 @@ static int run_centre(const Sys *S, int C, const double *radius, Sink *k, Oracle
             g_dec.count = 0;
             g_dec.flip = 0;
             memset(chi, 0, sizeof(double) * NCUM(la) * NCUM(lb));
+            memset(chiAbs, 0, sizeof(double) * NCUM(la) * NCUM(lb));
+            g_abs = k->scale ? chiAbs : NULL;
             if (type == 1) type1_block(S, &cc, sa, sb, ws, we, chi, st);
             else type2_block(S, &cc, sa, sb, ws, we, chi, st);
+            g_abs = NULL;
             poly_shift(S, chi, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm, blk, st);
+            if (k->scale && k->nBlocks < k->maxBlocks)
+              k->scale[k->nBlocks] = poly_shift_abs(S, chiAbs, la, cc.uspA[A], dA, lb, cc.uspA[B], dB, norm);
             emit(S, k, C, sa, sb, type, blk);
             const int m = g_dec.count;
             if (!k->alt || m == 0) continue;
@@ -1450,6 +1504,7 @@ static int run_centre(const Sys *S, int C, const double *radius, Sink *k, Oracle
           g_dec.track = 0;
         }
   free(chi);
+  free(chiAbs);
   free(blk);
   centre_free(&cc, S->nAtoms);
   return status;
@@ -1520,13 +1575,13 @@ int oracle_blocks(SYS_ARGS, int centerLo, int centerHi, int maxBlocks, int *meta
 }
 
 int oracle_blocks_alt(SYS_ARGS, int centerLo, int centerHi, double kappa, int maxBlocks,
-                      int *meta, long long maxData, double *data, int *nBlocks,
+                      int *meta, long long maxData, double *data, double *scale, int *nBlocks,
                       long long *nData, int maxAlt, int *altMeta, long long maxAltData,
                       double *altData, int *nAlt, long long *nAltData, OracleStats *stats) {
   Sink k, a;
   memset(&k, 0, sizeof k);
   memset(&a, 0, sizeof a);
-  k.maxBlocks = maxBlocks; k.meta = meta; k.maxData = maxData; k.data = data;
+  k.maxBlocks = maxBlocks; k.meta = meta; k.maxData = maxData; k.data = data; k.scale = scale;
   a.maxBlocks = maxAlt; a.meta = altMeta; a.maxData = maxAltData; a.data = altData;
   k.alt = &a;
   g_dec.kappa = kappa;

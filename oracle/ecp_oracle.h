@@ -81,7 +81,10 @@ int oracle_blocks(int nrAtoms, const double *geometry,
  * quadratures took a convergence decision within rounding noise (the test's
  * two sides closer than kappa * 2^-53 * sum |w f| allows), the block
  * recomputed with chosen such decisions inverted, recorded with the same
- * meta rows into altMeta / altData (several per block possible). */
+ * meta rows into altMeta / altData (several per block possible).  scale (one
+ * per block, or NULL): the largest element of the block evaluated over
+ * absolute values (the angular contractions and the shift onto A and B with
+ * |factor| and |term|), which sets the size of any FP64 evaluation's rounding. */
 int oracle_blocks_alt(int nrAtoms, const double *geometry,
                       const int *shellsECP, const int *KECP, const int *lECP,
                       const double *nECP, const double *dECP, const double *aECP,
@@ -89,8 +92,8 @@ int oracle_blocks_alt(int nrAtoms, const double *geometry,
                       const double *dBS, const double *aBS,
                       int largeGridOrder, double tolerance, double accuracy,
                       int centerLo, int centerHi, double kappa, int maxBlocks, int *meta,
-                      long long maxData, double *data, int *nBlocks, long long *nData,
-                      int maxAlt, int *altMeta, long long maxAltData, double *altData,
+                      long long maxData, double *data, double *scale, int *nBlocks,
+                      long long *nData, int maxAlt, int *altMeta, long long maxAltData, double *altData,
                       int *nAlt, long long *nAltData, OracleStats *stats);
 
 int oracle_getIntegrals_mt(int nrAtoms, const double *geometry,

@@ -71,7 +71,7 @@ def oracle_lib():
                                                         ct.POINTER(ct.c_longlong),
                                                         ct.POINTER(OracleStats)]
         lib.oracle_blocks_alt.argtypes = _sys_argtypes() + [ct.c_int, ct.c_int, ct.c_double, ct.c_int, _I,
-                                                            ct.c_longlong, _D, _I,
+                                                            ct.c_longlong, _D, _D, _I,
                                                             ct.POINTER(ct.c_longlong), ct.c_int, _I,
                                                             ct.c_longlong, _D, _I,
                                                             ct.POINTER(ct.c_longlong),
@@ -122,13 +122,16 @@ def oracle_blocks(s, centre_lo=0, centre_hi=None, with_stats=False):
 def oracle_blocks_alt(s, kappa=16.0, centre_lo=0, centre_hi=None):
     """oracle_blocks plus the alternative blocks of decisions taken within
     rounding noise (see decide() in ecp_oracle.c): returns (rc, meta, data,
-    alt_meta, alt_data); alt rows carry the meta of the block they replace."""
+    alt_meta, alt_data, scale); alt rows carry the meta of the block they
+    replace; scale[i] is block i's largest element evaluated over absolute
+    values (its rounding-error scale)."""
     lib = oracle_lib()
     hi = s.n_atoms if centre_hi is None else centre_hi
     ncent = int(np.count_nonzero(s.shellsECP[centre_lo:hi]))
     mb, md = _capacity(s, ncent)
     meta = np.zeros(8 * mb, dtype=np.int32)
     data = np.zeros(md, dtype=np.float64)
+    scale = np.zeros(mb, dtype=np.float64)
     for grow in (2, 20):  # alternatives per block: up to 19 (see run_centre)
         ma, mda = grow * mb + 64, grow * md + 4096
         ameta = np.zeros(8 * ma, dtype=np.int32)
@@ -137,22 +140,24 @@ def oracle_blocks_alt(s, kappa=16.0, centre_lo=0, centre_hi=None):
         nd, nad = ct.c_longlong(0), ct.c_longlong(0)
         st = OracleStats()
         rc = lib.oracle_blocks_alt(*_sys_args(s), centre_lo, hi, float(kappa), mb, meta.ctypes.data_as(_I),
-                                   md, data.ctypes.data_as(_D), ct.byref(nb), ct.byref(nd), ma,
+                                   md, data.ctypes.data_as(_D), scale.ctypes.data_as(_D), ct.byref(nb),
+                                   ct.byref(nd), ma,
                                    ameta.ctypes.data_as(_I), mda, adata.ctypes.data_as(_D), ct.byref(na),
                                    ct.byref(nad), ct.byref(st))
         if rc != -2:
             break
     return (rc, meta[:8 * nb.value].reshape(-1, 8).copy(), data[:nd.value].copy(),
-            ameta[:8 * na.value].reshape(-1, 8).copy(), adata[:nad.value].copy())
+            ameta[:8 * na.value].reshape(-1, 8).copy(), adata[:nad.value].copy(), scale[:nb.value].copy())
 
 
-def match_blocks(meta, data, ref_meta, ref_data, alt_meta=None, alt_data=None, bar=None):
+def match_blocks(meta, data, ref_meta, ref_data, alt_meta=None, alt_data=None, bar=None, scale=None):
     """Compares blocks in callback order against the reference blocks.
 
     A block passes when its largest element difference from the reference
     block is within bar(block), or from one of the block's alternatives (the
     reference's results with a decision taken within rounding noise
-    inverted).  bar(ref_block) -> allowed absolute difference.  Returns a
+    inverted).  bar(ref_block) -> allowed absolute difference, or
+    bar(ref_block, scale_i) when the blocks' scales are given.  Returns a
     dict: n_blocks, n_alt_used, worst (largest diff / bar over the passing
     choice), failures (list of (meta row, diff, bar)), max_abs."""
     assert np.array_equal(meta, ref_meta), "block lists differ"
@@ -165,11 +170,11 @@ def match_blocks(meta, data, ref_meta, ref_data, alt_meta=None, alt_data=None, b
             off += n
     out = {"n_blocks": len(meta), "n_alt_used": 0, "worst": 0.0, "failures": [], "max_abs": 0.0}
     off = 0
-    for m in meta:
+    for i, m in enumerate(meta):
         n = ((m[2] + 1) * (m[2] + 2) // 2) * ((m[5] + 1) * (m[5] + 2) // 2)
         g, r = data[off:off + n], ref_data[off:off + n]
         off += n
-        b = bar(r)
+        b = bar(r) if scale is None else bar(r, scale[i])
         d = float(np.max(np.abs(g - r))) if n else 0.0
         if d > b:
             for a in alts.get(tuple(int(x) for x in m), []):

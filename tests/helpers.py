@@ -65,3 +65,41 @@ def one_centre_answers():
 
 def max_rel(a, b):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+# Bar for configurations with g shells and large exponents (elements up to
+# 6e9; the shift onto A and B sums terms up to ~1e7 times larger than the
+# block).  Any correct FP64 evaluation of a block differs from another by a
+# few units of 2^-53 times the block's scale -- its largest element
+# evaluated over absolute values, which the oracle returns with
+# oracle_blocks_alt (measured: at most 3.7 units between the oracle and
+# either GPU path on the mixed batch and the sweep).  The bar is TOL_ABS
+# plus 128 units; blocks without cancellation and below 1e3 keep the 1e-10
+# absolute bar.
+SCALE_UNITS = 128.0
+
+
+def bar_scaled(ref_block, scale) -> float:
+    return TOL_ABS + SCALE_UNITS * 2.0 ** -53 * float(scale)
+
+
+# Rounding-noise bound (in units of 2^-53 times the sum of |w f| of a
+# quadrature) within which the oracle marks a convergence decision as
+# ambiguous and offers the inverted branch (oracle_blocks_alt).  The GPU
+# paths evaluate the integrands with other (correct) roundings: CUDA's exp,
+# the batched path's Horner Bessel rows and table exp, contracted multiply-adds.
+KAPPA_FP64 = 128.0
+
+
+def size_preserving_subset(s, centres, basis_atoms):
+    """s.subset with, in addition, one atom carrying a shell of the system's
+    largest l and the centre with its largest ECP L, so that the reference's
+    global table sizes -- and with them the values its fallbacks read from
+    stale buffers -- are those of the full system."""
+    lmax, Lmax = s.max_l_basis(), s.max_l_ecp()
+    starts = np.concatenate([[0], np.cumsum(s.shellsBS)]).astype(int)
+    G = next(a for a in range(s.n_atoms) if np.any(s.lBS[starts[a]:starts[a + 1]] == lmax))
+    est = np.concatenate([[0], np.cumsum(s.shellsECP)]).astype(int)
+    CL = next(a for a in range(s.n_atoms)
+              if s.shellsECP[a] and int(np.max(s.lECP[est[a]:est[a + 1]])) == Lmax)
+    return s.subset(centres=sorted(set(centres) | {CL}), basis_atoms=sorted(set(basis_atoms) | {G}))

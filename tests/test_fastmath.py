@@ -32,7 +32,15 @@ int main() {
   }
   double sub = 0;
   for (double x = -745.0; x < -708.0; x += 0.001) sub = std::fmax(sub, std::fabs(ecpgb::fast_exp(x) - std::exp(x)));
-  std::printf("%ld %.1f %.17g %.3g %.17g %.17g\n", n, worst, at, sub, ecpgb::fast_exp(0.0), ecpgb::fast_exp(-1e-20));
+  // the overflow threshold: finite (within 2 ulp) up to ln(DBL_MAX), infinite above
+  int over = 0;
+  for (double x = 709.7; x < 709.79; x += 1e-5) {
+    double a = ecpgb::fast_exp(x), b = std::exp(x);
+    if (std::isinf(a) != std::isinf(b) || (!std::isinf(b) && std::fabs((double)(ord(a) - ord(b))) > 2.0)) over++;
+  }
+  const double lnmax = 0x1.62e42fefa39efp+9;
+  over += std::isinf(ecpgb::fast_exp(lnmax)) + !std::isinf(ecpgb::fast_exp(std::nextafter(lnmax, 800.0)));
+  std::printf("%ld %.1f %.17g %.3g %.17g %.17g %d\n", n, worst, at, sub, ecpgb::fast_exp(0.0), ecpgb::fast_exp(-1e-20), over);
   return 0;
 }
 """
@@ -53,3 +61,4 @@ def test_fast_exp_against_libm(tmp_path):
     assert worst <= 2.0, f"max error {worst} ulp at x = {out[2]}"
     assert sub < 1e-320
     assert float(out[4]) == 1.0 and float(out[5]) == 1.0
+    assert int(out[6]) == 0, "overflow threshold differs from exp's"

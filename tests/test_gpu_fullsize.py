@@ -1,0 +1,95 @@
+"""Full-size parity on the two large configurations: the mixed batch
+(200 shells, 20,100 pairs, l <= 4, contraction 1-10, exponents 0.02-200, 10
+ECP centres) and the high-accuracy sweep (447 shells, 99,681 pairs, l <= 4, L
+<= 5 with 6 terms, exponents 0.01-500).
+
+The whole workload runs on the GPU in both FP64 paths (plain drop-in and
+batched); a seeded sample of sub-systems -- one ECP centre and three basis
+atoms, plus the atoms that keep the full system's table sizes -- is computed
+by the oracle, and every block of the sample is compared with the GPU's block
+of the same (centre, shell pair) from the full run.
+
+Bar: helpers.bar_scaled (1e-10, plus 128 * 2^-53 of the block's scale, its
+largest element evaluated over absolute values: the rounding any correct FP64
+evaluation carries where the shift onto A and B cancels terms ~1e7 times
+larger than the result).
+Decisions the reference takes within rounding noise (a quadrature's error
+test within helpers.KAPPA_FP64 * 2^-53 * sum |w f| of its tolerance) can go
+either way in another correct FP64 evaluation; a block also passes when it
+matches the oracle's block with such decisions inverted (oracle_blocks_alt).
+The number of blocks that took the other branch is bounded as well."""
+import multiprocessing as mp
+
+import numpy as np
+import pytest
+
+from libecp_gb300 import workloads as W
+from oracle import oracle as O
+from tests.helpers import KAPPA_FP64, bar_scaled, size_preserving_subset
+
+pytestmark = pytest.mark.gpu
+
+N_PIECES = 8
+
+
+def _pieces(name):
+    s = W.mixed_batch(0) if name == "mixed" else W.large_sweep(0)
+    rng = np.random.default_rng(11 if name == "mixed" else 12)
+    centres = [a for a in range(s.n_atoms) if s.shellsECP[a]]
+    basis = [a for a in range(s.n_atoms) if s.shellsBS[a]]
+    out = []
+    for _ in range(N_PIECES):
+        c = int(rng.choice(centres))
+        atoms = [int(a) for a in rng.choice(basis, size=3, replace=False)]
+        out.append((name, c, atoms))
+    return out
+
+
+def _oracle_piece(args):
+    name, c, atoms = args
+    s = W.mixed_batch(0) if name == "mixed" else W.large_sweep(0)
+    sub = size_preserving_subset(s, [c], atoms)
+    return O.oracle_blocks_alt(sub, KAPPA_FP64)
+
+
+@pytest.fixture(scope="module")
+def eg():
+    import libecp_gb300
+    libecp_gb300.lib()
+    return libecp_gb300
+
+
+@pytest.mark.parametrize("name", ["mixed", "sweep"])
+def test_full_size_sampled_against_oracle(eg, name):
+    pieces = _pieces(name)
+    with mp.get_context("spawn").Pool(min(len(pieces), mp.cpu_count())) as pool:
+        oracle = pool.map_async(_oracle_piece, pieces)
+        s = W.mixed_batch(0) if name == "mixed" else W.large_sweep(0)
+        units = eg.unit_table(s)
+        index = {(u[6], u[0], u[1], u[3], u[4]): i for i, u in enumerate(units)}
+        gpu = {mode: eg.raw_blocks(s, mode) for mode in (eg.ECPGB_FP64, eg.ECPGB_FAST)}
+        results = oracle.get()
+    report = []
+    for mode, (v, offs, st, info) in gpu.items():
+        n_blocks = n_alt = 0
+        failures = []
+        for rc, meta, data, am, ad, scale in results:
+            assert rc == 0 and len(meta)
+            got = []
+            for m in meta:
+                A, s1, la, B, s2, lb, C, typ = (int(x) for x in m)
+                u = index[(C, A, s1, B, s2)]
+                assert st[u] != eg.UNIT_SKIPPED
+                n = ((la + 1) * (la + 2) // 2) * ((lb + 1) * (lb + 2) // 2)
+                got.append(v[offs[u] + (typ - 1) * n: offs[u] + typ * n])
+            res = O.match_blocks(meta, np.concatenate(got), meta, data, am, ad, bar_scaled, scale)
+            failures += [(f[0], f"{f[1]:.3e}", f"{f[2]:.3e}", int(st[index[(f[0][6], f[0][0], f[0][1], f[0][3],
+                                                                              f[0][4])]]))
+                         for f in res["failures"]]
+            n_blocks += res["n_blocks"]
+            n_alt += res["n_alt_used"]
+        report.append((mode, n_blocks, n_alt, failures))
+    # every block within the bar; the other branch of a noise-level decision
+    # is the exception
+    assert all(not r[3] for r in report), report
+    assert all(r[2] <= max(2, r[1] // 200) for r in report), report

@@ -120,14 +120,15 @@ def test_alternatives_leave_the_reference_branch_unchanged():
     rc, m0, d0 = O.oracle_blocks(s)
     counts = []
     for kappa in (0.0, 16.0, 1e6):
-        rc2, m, d, am, ad = O.oracle_blocks_alt(s, kappa)
+        rc2, m, d, am, ad, sc = O.oracle_blocks_alt(s, kappa)
+        assert np.all(sc >= np.array([np.max(np.abs(d[o:o + n])) for o, n in _spans(m)]) * (1 - 1e-12))
         assert rc2 == rc and np.array_equal(m, m0) and np.array_equal(d, d0)
         counts.append(len(am))
         keys = {tuple(r) for r in m.tolist()}
         assert all(tuple(r) in keys for r in am.tolist())
     assert counts[0] == 0 and counts[0] <= counts[1] <= counts[2] and counts[2] > 0
     # the matcher: a block equal to an alternative passes, a perturbed one does not
-    rc2, m, d, am, ad = O.oracle_blocks_alt(s, 1e6)
+    rc2, m, d, am, ad, sc = O.oracle_blocks_alt(s, 1e6)
     n0 = ((am[0][2] + 1) * (am[0][2] + 2) // 2) * ((am[0][5] + 1) * (am[0][5] + 2) // 2)
     off = 0
     for row in m:
@@ -143,3 +144,11 @@ def test_alternatives_leave_the_reference_branch_unchanged():
     g[off] += 1.0
     res = O.match_blocks(m, g, m, d, am, ad, bar)
     assert len(res["failures"]) == 1
+
+
+def _spans(meta):
+    off = 0
+    for m in meta:
+        n = ((m[2] + 1) * (m[2] + 2) // 2) * ((m[5] + 1) * (m[5] + 2) // 2)
+        yield off, n
+        off += n
