@@ -146,6 +146,27 @@ print(json.dumps({{"t": time.perf_counter() - t0}}))
 """
 
 
+def host_cores() -> int:
+    """Cores this process may run on (the affinity mask, not the machine's count)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
+def run_cpu_single(system, workload="cluster"):
+    """The port on one core over a quarter of the bounded sample (its first
+    centres): units/s, the number of units and the seconds."""
+    from oracle import oracle as O
+    sample, text = cpu_sample_system(system, workload)
+    cs = [a for a in range(sample.n_atoms) if sample.shellsECP[a] > 0]
+    part = sample.subset(centres=cs[:max(1, len(cs) // 4)])
+    t0 = time.perf_counter()
+    rc, I, st = O.oracle_matrix(part, nthreads=1, with_stats=True)
+    t = time.perf_counter() - t0
+    return st["blocks"] / t, st["blocks"], t
+
+
 def run_cpu_baseline(system, threads, workload="cluster", seed=0):
     """Times the reference's CPU path on the sample, on this machine's cores.
 
@@ -258,42 +279,55 @@ def ours(args, rank, world):
         serving = serving_run(eg, args.serve_rate, args.serve_seconds)
 
     mixed = None
-    if rank == 0 and args.mixed_report:
-        # the mixed-precision mode on the same job: speed and error per L class
-        from libecp_gb300.precision import class_errors
+    if rank == 0 and args.mixed_report and mode != eg.ECPGB_FP64:
+        # the mixed-precision path on the same job: speed, its error against
+        # the plain FP64 path over every unit, and per L class against the
+        # oracle on the job's first two ECP centres
+        from libecp_gb300.precision import oracle_class_errors
         mj = eg.Job(system, mode=eg.ECPGB_MIXED)
-        mj.tune()
-        mj.run(1, flush_l2=True)
-        mms, _ = mj.run(2, flush_l2=True)
+        mchosen, _ = mj.tune()
+        mj.run(args.warmup, flush_l2=True)
+        mms, mmu = mj.run(args.steps, flush_l2=True)
         mj.close()
-        rep = class_errors(system, eg.raw_blocks(system, eg.ECPGB_FP64), eg.raw_blocks(system, eg.ECPGB_MIXED))
-        mixed = {"value": total_units / (float(np.mean(mms)) / 1e3), "unit": UNIT,
-                 "vs_batched_fp64": (total_units / (float(np.mean(mms)) / 1e3)) / value,
-                 "statuses_equal_fp64": rep["statuses_equal"],
-                 "error_vs_fp64_per_l_class": rep["classes"]}
+        mval = total_units / (float(np.mean(mms)) / 1e3)
+        v1, o1, st1, _ = eg.raw_blocks(system, eg.ECPGB_FP64)
+        v3, o3, st3, _ = eg.raw_blocks(system, eg.ECPGB_MIXED)
+        cs = [a for a in range(system.n_atoms) if system.shellsECP[a] > 0]
+        rep = oracle_class_errors(system.subset(centres=cs[:2]), eg.ECPGB_MIXED)
+        mixed = {"value": mval, "unit": UNIT, "ms_per_step": float(np.mean(mms)),
+                 "unit_kernel_ms": float(np.mean(mmu)), "launch_config": mchosen,
+                 "vs_batched_fp64": mval / value, "vs_plain_fp64": (mval / plain) if plain else None,
+                 "max_abs_error_vs_plain_fp64_all_units": float(np.max(np.abs(v3 - v1))),
+                 "statuses_equal_fp64": bool(np.array_equal(st1, st3)),
+                 "error_vs_oracle_per_l_class_first_2_centres": rep["classes"]}
 
     line = None
     if rank == 0:
-        cores = os.cpu_count() or 1
-        cpu_v, kind, st, text, s_units, s_time = run_cpu_baseline(system, min(cores, 16), args.workload, rank)
+        cores = host_cores()
+        cpu_v, kind, st, text, s_units, s_time = run_cpu_baseline(system, cores, args.workload, rank)
+        cpu1_v, cpu1_units, cpu1_t = run_cpu_single(system, args.workload)
         f_unit = algorithmic_flops(st) / max(st["blocks"], 1)
-        achieved = f_unit * emitted / (t_unit / 1e3) / 1e12
+        alg_achieved = f_unit * emitted / (t_unit / 1e3) / 1e12
         peak = peaks["fp64_fma_tflops"]
         if mode == eg.ECPGB_FP64:
             kernel = "k_unit"
         else:
             kernel = "k_unit_queue" if tuned["chosen"]["queue"] else "k_unit_fast"
-        traffic = None
-        pipe = None
+        # executed work: FP64 operations the unit kernel executed per emitted
+        # unit (ncu: 2 DFMA + DMUL + DADD thread instructions of one launch on
+        # the cluster's first 8 centres, divided by its emitted units), FP64
+        # pipe utilisation and DRAM bytes, from profiles/roofline_inputs.txt
+        entry = {}
         prof = os.path.join(ROOT, "profiles", "roofline_inputs.txt")
         if os.path.exists(prof):
             with open(prof) as f:
-                # the two batched kernels run the same unit code
-                entry = json.load(f).get("k_unit_fast" if kernel == "k_unit_queue" else kernel, {})
-            per_unit = entry.get("dram_bytes_per_emitted_unit")
-            pipe = entry.get("fp64_pipe_active")
-            if per_unit:  # ncu dram read+write of one unit-kernel launch, scaled to this launch
-                traffic = per_unit * emitted
+                inputs = json.load(f)
+            key = {"k_unit": "k_unit", "k_unit_queue": "k_unit_queue", "k_unit_fast": "k_unit_queue"}[kernel]
+            entry = inputs.get(key + ("_mixed" if mode == eg.ECPGB_MIXED else ""), {})
+        f_exec = entry.get("fp64_flops_per_emitted_unit")
+        achieved = f_exec * emitted / (t_unit / 1e3) / 1e12 if f_exec else None
+        traffic = entry["dram_bytes_per_emitted_unit"] * emitted if entry.get("dram_bytes_per_emitted_unit") else None
+        pipe = entry.get("fp64_pipe_active")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
@@ -311,24 +345,27 @@ def ours(args, rank, world):
                     "d2h_bytes_per_step": int(d2h),
                     "api": "ecpgb_getIntegrals (the getIntegrals call, host buffers, path = mode)"},
             "roofline": {"bound": "fp64", "kernel": kernel,
-                         "achieved": achieved,
-                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if achieved else None,
                          "traffic": traffic,
-                         "peak_source": "FP64 FMA pipe measured live by ecpgb_measure_peaks",
-                         "alg_flops_per_unit": f_unit, "unit_kernel_ms": t_unit,
-                         # F_alg counts the reference's full large-grid tabulation of every
-                         # fallback; the batched kernel stops at the converged level, so the
-                         # executed work is the ncu FP64 pipe utilisation below
+                         "peak_source": "FP64 FMA pipe measured live by ecpgb_measure_peaks (of measured)",
+                         "executed_fp64_flops_per_unit": f_exec,
                          "fp64_pipe_active_ncu": pipe,
-                         "note": ("F_alg is the reference's work (its control flow counted by the oracle), "
-                                  "including the full 1023-point large-grid tabulation of every fallback; "
-                                  "the batched kernel tabulates only the levels up to convergence and only "
-                                  "the points whose values are not negligible, with the same quadrature "
-                                  "results, so frac can exceed 1; the executed FP64 work is "
-                                  "fp64_pipe_active_ncu" if kernel != "k_unit" else
-                                  "F_alg is the reference's work, counted by the oracle on its control flow")},
-            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": min(cores, 16), "kind": kind,
-                             "sample": f"{text}: {s_units} units in {s_time:.1f} s"},
+                         "unit_kernel_ms": t_unit,
+                         "alg_flops_per_unit": f_unit, "alg_achieved": alg_achieved,
+                         "alg_frac": alg_achieved / peak,
+                         "inputs": entry.get("source"),
+                         "note": ("achieved = FP64 operations the kernel executed (ncu counts per emitted "
+                                  "unit on the cluster's first 8 centres) x emitted units / the unit kernel's "
+                                  "CUDA-event time; alg_* = the reference's work counted by the oracle on its "
+                                  "control flow, which includes the full 1023-point tabulation of every "
+                                  "large-grid fallback the kernel skips, so alg_frac can exceed 1")},
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"{text}: {s_units} units in {s_time:.1f} s on {cores} threads "
+                                       f"(ECP centres dealt round-robin to threads)",
+                             "single_core": {"value": cpu1_v, "cores": 1,
+                                             "sample": f"the first quarter of the sample's centres: "
+                                                       f"{cpu1_units} units in {cpu1_t:.1f} s"}},
             "clocks": clk.summary(),
             "serving": serving,
             "mixed_precision": mixed,
@@ -365,7 +402,7 @@ def reference_arm(args, rank, world):
     from libecp_gb300 import workloads as W
     from oracle import oracle as O
     system = W.batched_cluster(seed=0)
-    cores = min(os.cpu_count() or 1, 16)
+    cores = host_cores()
     vals = []
     for i in range(args.warmup + args.steps):
         v, kind, st, text, units, t = run_cpu_baseline(system, cores)
@@ -399,8 +436,8 @@ def main():
     ap.add_argument("--workload", default="cluster", choices=list(WORKLOADS),
                     help="cluster (the headline), cluster8 (its first 8 centres: profiler captures), "
                          "mixed_batch and sweep (the other configurations)")
-    ap.add_argument("--mixed-report", type=int, default=0,
-                    help="also run the mixed-precision mode and report its error per L class")
+    ap.add_argument("--mixed-report", type=int, default=1,
+                    help="also run the mixed-precision mode and report its speed and errors")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -22,6 +22,8 @@
 
 #include <cstdint>
 
+#include "ecp_ff.h"
+
 namespace ecpgb {
 
 constexpr int kSmallOrder = 383;       // PS93(128) abscissae
@@ -72,7 +74,10 @@ struct DevJob {
   // whose index differs across a warp (the __constant__ copies serialise those)
   const int *s93, *s92;
   const short *byN93;          // small-grid slots step by step in ascending point order
-  const float *besHf;          // besH in FP32 (mixed mode)
+  // mixed path: tables as float pairs (ecp_ff.h)
+  const ff *besHf, *besAf, *besZf;  // besH, besA, besZ
+  const ff *xLf, *wLf;              // large grid abscissae and weights
+  const ff *termAf, *termDf;        // ECP term exponents and coefficients
   const double *besZ;          // Bessel table abscissae i / (besselN / 16)
   int besHL;
   const double *shNorm;        // spherical-harmonic normalisation [l][m], side tmDim + 1
@@ -96,7 +101,7 @@ struct DevJob {
   unsigned long long *queueHead; // next queue position (persistent launch); reset per run
   int gcap;                      // type-1 step-table width cap (doubles per slot per warp)
   int maxNP;                     // most primitive pairs of a shell pair (shared-memory sizing)
-  int mixed;                     // 1: FP32 Bessel Taylor rows and ECP channel terms
+  int mixed;                     // 1: the fallbacks' tables and sums in double-single (ecp_ff.h)
   int balance;                   // 1: type-1 groups narrowed so that every warp gets pairs
   // screening stage (batched path): the queue of units that compute blocks
   int *live;                     // live units in queue order (null: no screening stage)

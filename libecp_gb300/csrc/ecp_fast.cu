@@ -43,14 +43,6 @@ constexpr int kLargeWords = (kMaxLargeOrder + 1) / 32;  // bitmap words over the
 static_assert(kLargeWords * 32 >= kMaxLargeOrder && kLargeWords % 2 == 0, "large-grid bitmap size");
 
 
-// Mixed mode: FP32 integrands carry noise of a few 1e-8 relative, below which
-// no error estimate can fall, so a quadrature also stops once its estimated
-// error is below kMixedRel of its value -- from kMixedMinPoints points on
-// only, because the successive-difference estimates of the first levels can
-// vanish by coincidence (the FP64 modes pass rel = 0).
-constexpr double kMixedRel = 1e-6;
-constexpr int kMixedMinPoints = 63;
-
 // --------------------------------------------------------------- helpers
 
 // K_0..K_lmax(z): the branches of src/bessel.c:102-199.  The Taylor branch
@@ -91,21 +83,6 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
     const double h = J.besselN / 16;  // integer division, as the reference
     const int index = (int)floor(z * h + 0.5);
     x = z - __ldg(J.besZ + index);  // index / h, tabulated
-    if constexpr (kMixed) {
-      // mixed mode: the Taylor rows in FP32 (every lane of the warp is on
-      // this branch or the large-argument one, which stays FP64)
-      const float *qf = J.besHf + (size_t)index * HL1 * 6;
-      const float xf = (float)x;
-      for (int l = 0; l <= lmax; l++) {
-        const float *q = qf + 6 * l;
-        float v = fmaf(q[5], xf, q[4]);
-        v = fmaf(v, xf, q[3]);
-        v = fmaf(v, xf, q[2]);
-        v = fmaf(v, xf, q[1]);
-        K[l * stride] = (double)fmaf(v, xf, q[0]);
-      }
-      return;
-    }
     cf = J.besH + (size_t)index * HL1 * 6;
     cs = 6;
   }
@@ -157,14 +134,6 @@ static __device__ double bessel_row(const DevJob &J, int l, double z) {
   return fma(v, dz, q[0]);
 }
 
-// One ECP term d r^n exp(-a r^2) in FP32 (mixed mode): n is an integer in
-// practice (0, 1, 2 in every basis set seen); other n take powf.
-static __device__ inline float term_f32(const DevJob &J, int t, float r, float r2) {
-  const double n = J.termN[t];
-  float p = n == 0.0 ? 1.0f : n == 1.0 ? r : n == 2.0 ? r * r : powf(r, (float)n);
-  return (float)J.termD[t] * p * expf(-(float)J.termA[t] * r2);
-}
-
 // U_l(r) of centre c for the channels l set in mask, in one pass over its
 // terms (src/ecp.c:42-60); the other entries of U are left untouched.
 template <bool kMixed>
@@ -172,17 +141,9 @@ static __device__ void channels_masked(const DevJob &J, int c, double r, unsigne
   double r2 = r * r;
   for (unsigned m = mask; m; m &= m - 1) U[__ffs(m) - 1] = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
-  if constexpr (kMixed) {
-    const float rf = (float)r, r2f = (float)r2;
-    for (int t = t0; t < t1; t++) {
-      int l = J.termL[t];
-      if (mask >> l & 1u) U[l] += (double)term_f32(J, t, rf, r2f);
-    }
-  } else {
-    for (int t = t0; t < t1; t++) {
-      int l = J.termL[t];
-      if (mask >> l & 1u) U[l] += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
-    }
+  for (int t = t0; t < t1; t++) {
+    int l = J.termL[t];
+    if (mask >> l & 1u) U[l] += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
   }
 }
 
@@ -190,17 +151,104 @@ template <bool kMixed>
 static __device__ double channel(const DevJob &J, int c, int l, double r) {
   double r2 = r * r, pot = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
-  if constexpr (kMixed) {
-    const float rf = (float)r, r2f = (float)r2;
-    float pf = 0.0f;
-    for (int t = t0; t < t1; t++)
-      if (J.termL[t] == l) pf += term_f32(J, t, rf, r2f);
-    return (double)pf;
-  } else {
-    for (int t = t0; t < t1; t++)
-      if (J.termL[t] == l) pot += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
-    return pot;
+  for (int t = t0; t < t1; t++)
+    if (J.termL[t] == l) pot += rpow(r, J.termN[t]) * J.termD[t] * fast_exp(-J.termA[t] * r2);
+  return pot;
+}
+
+// ------------------------------------------- double-single (mixed path)
+//
+// The mixed path evaluates the large-grid fallbacks' tables -- Bessel rows,
+// ECP channels, powers of r, the Gaussian prefactor -- and their integrand
+// products in double-single arithmetic (ecp_ff.h: FP32 pairs on the FMA
+// pipes), sums each level of a quadrature with a compensated FP32 sum and
+// adds it to the FP64 running sum at the level's end.  The convergence
+// tests, the level recurrences and every accumulation into T, Q and the
+// blocks stay FP64.  The fallbacks' test (PSM92, 16 e^2 <= 3 N |I - q| tol)
+// compares level differences far above the double-single rounding, so it
+// takes the FP64 path's decisions; the small-grid quadratures, whose
+// absolute test (err < tol) sits at the FP64 rounding level for large
+// integrals, are not touched.
+
+// 1 / z: the float reciprocal refined by one Newton step in ff.
+static __device__ inline ff ff_recip(ff z) {
+  const float y = __frcp_rn(z.hi);
+  const float e = __fmaf_rn(-z.lo, y, __fmaf_rn(-z.hi, y, 1.0f));  // 1 - z y
+  return ff_norm(y, __fmul_rn(y, e));
+}
+
+// K_0..K_lmax(z) in ff: the branches of bessel_fast over the tables' float
+// pairs (Taylor coefficients, table abscissae, large-argument polynomial).
+static __device__ void bessel_ff(const DevJob &J, int lmax, ff z, ff *K, int stride) {
+  if (__builtin_expect(z.hi < 1.0e-7f, 0)) {  // rare: the small-argument formula in FP64
+    double Kd[kMaxRows];
+    bessel_small(lmax, ff_to_double(z), Kd, 1);
+    for (int l = 0; l <= lmax; l++) K[l * stride] = ff_from_double(Kd[l]);
+    return;
   }
+  const int HL1 = J.besHL + 1;
+  if (z.hi > 16.0f || (z.hi == 16.0f && z.lo >= 0.0f)) {
+    const ff inv = ff_recip(z);
+    const ff mult = {0.5f * inv.hi, 0.5f * inv.lo}, x = ff_neg(mult);  // 1/(2z), -1/(2z)
+    const int cs = HL1 < 6 ? 6 : HL1;
+    for (int l = 0; l <= lmax; l++) {
+      const ff *q = J.besAf + (size_t)l * cs;
+      int k = l > 5 ? l : 5;
+      ff v = q[k];
+      while (k > 0) {
+        k--;
+        v = ff_add(ff_mul(v, x), q[k]);
+      }
+      K[l * stride] = ff_mul(v, mult);
+    }
+    return;
+  }
+  // the nearest table point; any neighbour would do as well (the Taylor
+  // series is accurate over the whole table step)
+  const int index = (int)floorf(__fmaf_rn(z.hi, (float)(J.besselN / 16), 0.5f));
+  const ff x = ff_add(z, ff_neg(J.besZf[index]));
+  const ff *qf = J.besHf + (size_t)index * HL1 * 6;
+  for (int l = 0; l <= lmax; l++) {
+    const ff *q = qf + 6 * l;
+    // the two top terms (below 1e-9 of the row) in FP32
+    ff v = ff_add(ff_mul_f(x, __fmaf_rn(q[5].hi, x.hi, q[4].hi)), q[3]);
+    v = ff_add(ff_mul(v, x), q[2]);
+    v = ff_add(ff_mul(v, x), q[1]);
+    K[l * stride] = ff_add(ff_mul(v, x), q[0]);
+  }
+}
+
+// One ECP term d r^n exp(-a r^2) in ff (r2 = r^2); terms below 2^-125 of
+// their coefficient are 0.
+static __device__ inline ff ecp_term_ff(const DevJob &J, int t, ff r, ff r2) {
+  const ff arg = ff_mul(J.termAf[t], r2);
+  if (arg.hi > 87.0f) return {0.0f, 0.0f};
+  const ff v = ff_mul(J.termDf[t], ff_exp(ff_neg(arg)));
+  const double n = J.termN[t];
+  if (n == 0.0) return v;
+  if (n == 1.0) return ff_mul(v, r);
+  if (n == 2.0) return ff_mul(v, r2);
+  return ff_mul(v, ff_from_double(rpow(ff_to_double(r), n)));  // other powers: rare
+}
+
+// U_l(r) in ff for the channels set in mask (the others untouched).
+static __device__ void channels_ff(const DevJob &J, int c, ff r, unsigned mask, ff *U) {
+  const ff r2 = ff_mul(r, r);
+  for (unsigned m = mask; m; m &= m - 1) U[__ffs(m) - 1] = {0.0f, 0.0f};
+  const int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
+  for (int t = t0; t < t1; t++) {
+    const int l = J.termL[t];
+    if (mask >> l & 1u) U[l] = ff_add(U[l], ecp_term_ff(J, t, r, r2));
+  }
+}
+
+static __device__ ff channel_ff(const DevJob &J, int c, int l, ff r) {
+  const ff r2 = ff_mul(r, r);
+  ff pot = {0.0f, 0.0f};
+  const int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
+  for (int t = t0; t < t1; t++)
+    if (J.termL[t] == l) pot = ff_add(pot, ecp_term_ff(J, t, r, r2));
+  return pot;
 }
 
 // Small-grid prefactor of a type-1 primitive pair, C1 = ca cb exp(zd2) with
@@ -274,7 +322,7 @@ static __device__ inline int step_end92(int s0) { return s0 == 0 ? 31 : s0 + 32;
 // large-grid schedule; `val(pos)` = w * f at slot pos; `vis(pos)` whether the
 // (upper) point counts.  State in I, p, q; returns through done/res.
 template <class V, class Vis>
-static __device__ inline void psm92_advance(int s0, int s1, double tol, double rel, V val, Vis vis,
+static __device__ inline void psm92_advance(int s0, int s1, double tol, V val, Vis vis,
                                             double &I, double &p, double &q, bool &done, double &res) {
   int pos = s0;
   if (pos == 0) {
@@ -296,10 +344,7 @@ static __device__ inline void psm92_advance(int s0, int s1, double tol, double r
     pos += 2;
     if (pos == c92_lvEnd[k]) {
       double N = c92_lvN[k] + 1.0, e = I - p;
-      // mixed mode: the reference's two-difference test with the tolerance
-      // raised to rel times the estimate
-      const double t = rel > 0.0 && N >= kMixedMinPoints ? fmax(tol, rel * fabs(16 * I / (3 * N))) : tol;
-      if (16 * e * e <= 3 * N * fabs(I - q) * t) {
+      if (16 * e * e <= 3 * N * fabs(I - q) * tol) {
         res = 16 * I / (3 * N);
         done = true;
       }
@@ -345,7 +390,7 @@ static __device__ bool ps93_walk_fast(const double *w, int start, int end, doubl
 // bit are skipped -- adding 0.0 changes no sum -- while every level end is
 // still visited in order for the convergence test.
 template <class V, class Vis>
-static __device__ inline void psm92_sparse(int s0, int s1, const unsigned *bits, double tol, double rel, V val,
+static __device__ inline void psm92_sparse(int s0, int s1, const unsigned *bits, double tol, V val,
                                            Vis vis, double &I, double &p, double &q, bool &done, double &res) {
   auto has = [&](int t) { return (bits[t >> 5] >> (t & 31)) & 1u; };
   int pos = s0;
@@ -385,14 +430,103 @@ static __device__ inline void psm92_sparse(int s0, int s1, const unsigned *bits,
     }
     if (pos == lvE) {
       double N = c92_lvN[k] + 1.0, e = I - p;
-      const double t = rel > 0.0 && N >= kMixedMinPoints ? fmax(tol, rel * fabs(16 * I / (3 * N))) : tol;
-      if (16 * e * e <= 3 * N * fabs(I - q) * t) {
+      if (16 * e * e <= 3 * N * fabs(I - q) * tol) {
         res = 16 * I / (3 * N);
         done = true;
       }
       k++;
     }
   }
+}
+
+// psm92_advance with val(pos) in ff: each level summed with a compensated
+// FP32 sum and added to the FP64 running sum I at the level's end (and at
+// the end of the slots walked, so that I is complete between calls).
+template <class V, class Vis>
+static __device__ inline void psm92_advance_ff(int s0, int s1, double tol, V val, Vis vis, double &I, double &p,
+                                               double &q, bool &done, double &res) {
+  int pos = s0;
+  if (pos == 0) {
+    I = ff_to_double(val(0));
+    p = I;
+    pos = 1;
+  }
+  int k = level_of(pos);
+  ff_acc acc;
+  while (pos < s1 && !done) {
+    int lvStart = k == 0 ? 1 : c92_lvEnd[k - 1];
+    if (pos == lvStart) {
+      q = 2 * p;
+      p = 2 * I;
+    }
+    acc.add(val(pos));
+    if (vis(pos + 1)) acc.add(val(pos + 1));
+    pos += 2;
+    if (pos == c92_lvEnd[k]) {
+      I += acc.value();
+      acc = ff_acc();
+      double N = c92_lvN[k] + 1.0, e = I - p;
+      if (16 * e * e <= 3 * N * fabs(I - q) * tol) {
+        res = 16 * I / (3 * N);
+        done = true;
+      }
+      k++;
+    }
+  }
+  I += acc.value();
+}
+
+// psm92_sparse with val(pos) in ff, levels summed as in psm92_advance_ff.
+template <class V, class Vis>
+static __device__ inline void psm92_sparse_ff(int s0, int s1, const unsigned *bits, double tol, V val, Vis vis,
+                                              double &I, double &p, double &q, bool &done, double &res) {
+  auto has = [&](int t) { return (bits[t >> 5] >> (t & 31)) & 1u; };
+  int pos = s0;
+  if (pos == 0) {
+    I = has(0) ? ff_to_double(val(0)) : 0.0;
+    p = I;
+    pos = 1;
+  }
+  int k = level_of(pos);
+  ff_acc acc;
+  while (pos < s1 && !done) {
+    const int lvStart = k == 0 ? 1 : c92_lvEnd[k - 1];
+    if (pos == lvStart) {
+      q = 2 * p;
+      p = 2 * I;
+    }
+    const int lvE = c92_lvEnd[k], stop = lvE < s1 ? lvE : s1;
+    while (true) {
+      int t = stop;  // first set bit in [pos, stop)
+      for (int w = pos >> 5; (w << 5) < stop; w++) {
+        unsigned word = bits[w];
+        if (w == (pos >> 5)) word &= ~0u << (pos & 31);
+        if (word) {
+          t = (w << 5) + __ffs(word) - 1;
+          break;
+        }
+      }
+      if (t >= stop) {
+        pos = stop;
+        break;
+      }
+      const int ps = (t - 1) | 1;  // the (lower, upper) pair holding t
+      if (has(ps)) acc.add(val(ps));
+      if (has(ps + 1) && vis(ps + 1)) acc.add(val(ps + 1));
+      pos = ps + 2;
+    }
+    if (pos == lvE) {
+      I += acc.value();
+      acc = ff_acc();
+      double N = c92_lvN[k] + 1.0, e = I - p;
+      if (16 * e * e <= 3 * N * fabs(I - q) * tol) {
+        res = 16 * I / (3 * N);
+        done = true;
+      }
+      k++;
+    }
+  }
+  I += acc.value();
 }
 
 // --------------------------------------------------------------- layout
@@ -591,7 +725,6 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
                                     const double *gA, const double *gB, int ws, int we, int pa0, int pb0,
                                     int &warn) {
   const int lane = threadIdx.x & 31, lab = la + lb, lq = lab + 1, O = kSmallOrder;
-  const double rel = kMixed ? kMixedRel : 0.0;
   // odd entry strides: lanes touching neighbouring entries hit distinct banks
   const int OL = J.largeOrder, TSs = 1 + 2 * lq, TSf = 3 + 2 * lq, RQ = lq * lq, nq = t1_items(lab);
   double *sc = W + L.w1Sc, *rsh = W + L.w1Rsh, *Q = W + L.w1Q, *H = W + L.w1H, *tab = W + L.w1Tab;
@@ -741,7 +874,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
           // of the threshold)
           const double d = fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q));
           q = (1 - j) * q + j * I;
-          if (cnt > 0 && (16 * d < J.tol * (3 * n) || (rel > 0.0 && n >= kMixedMinPoints && d < rel * fabs(q)))) {
+          if (cnt > 0 && 16 * d < J.tol * (3 * n)) {
             done = true;
             Q[g * RQ + l1 * lq + l2] += 16 * q / (3 * n);
           }
@@ -764,8 +897,10 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
                  cb = zeta_times(pcB[kk % Nb], zb, pb0);
     const double s = sc[gg * 6], z = -za - zb, zd2 = -za * dAC * dAC - zb * dBC * dBC;
     const double C2 = ca * cb;
+    const ff C2f = ff_from_double(C2), sf = ff_from_double(s);
     double i1, i2;
     fm06(za, zb, dAC, dBC, i1, i2);
+    const ff i1f = ff_from_double(i1);
     // first point past both centres whose exponent is below the screen
     // (src/type1.c:168-176).  Past both centres the exponent falls as r
     // grows, so the predicate is monotone in the index: a 32-way search,
@@ -810,13 +945,27 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
         if (n < nb && !(upper && n > end)) {
           double r = i1 * J.xLarge[n] + i2, ex = (z * r + s) * r + zd2;
           if (ex >= J.lnAcc1) {
-            double v = w * (C2 * channel<kMixed>(J, c, Lc, r) * fast_exp(ex));
-            any = v != 0.0;
-            bessel_fast<kMixed>(J, kq, s * r, K, 1);
-            WR[0] = v;
-            for (int l = 1; l <= rq; l++) {
-              v *= r;
-              WR[l] = v;
+            if constexpr (kMixed) {
+              ff *Kf = (ff *)K, *WRf = (ff *)WR;
+              const ff rf = ff_from_double(r);
+              ff v = ff_mul(ff_mul(J.wLf[n], i1f),
+                            ff_mul(C2f, ff_mul(channel_ff(J, c, Lc, rf), ff_exp(ff_from_double(ex)))));
+              any = v.hi != 0.0f;
+              bessel_ff(J, kq, ff_mul(sf, rf), Kf, 1);
+              WRf[0] = v;
+              for (int l = 1; l <= rq; l++) {
+                v = ff_mul(v, rf);
+                WRf[l] = v;
+              }
+            } else {
+              double v = w * (C2 * channel<kMixed>(J, c, Lc, r) * fast_exp(ex));
+              any = v != 0.0;
+              bessel_fast<kMixed>(J, kq, s * r, K, 1);
+              WR[0] = v;
+              for (int l = 1; l <= rq; l++) {
+                v *= r;
+                WR[l] = v;
+              }
             }
           }
         } else if (__builtin_expect(n != nb && !upper && n < O && n >= ws && n < we, 0)) {
@@ -835,21 +984,34 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
               WR[l] = ok ? v * pw : 0.0;
               K[l] = ok ? bessel_row(J, lr, s * xr) : 0.0;
             }
+            if constexpr (kMixed)  // the rows as ff, in place (entry l holds row l either way)
+              for (int l = 0; l <= lab; l++) {
+                ((ff *)WR)[l] = ff_from_double(WR[l]);
+                ((ff *)K)[l] = ff_from_double(K[l]);
+              }
           }
         }
-        if (!any) {
+        if (!any) {  // zero bits read as 0.0 in FP64 and in ff alike
           for (int l = 0; l <= kq; l++) K[l] = 0.0;
           for (int l = 0; l <= rq; l++) WR[l] = 0.0;
         }
       }
       __syncwarp();
       if (!done2) {
-        auto val = [&](int t) {
-          const double *e = tab + (t - s0) * TSf;
-          return e[lq + l1] * e[l2];
-        };
         auto vis = [&](int t) { return c92_slot[t] <= end; };
-        psm92_advance(s0, s1, J.tol, kMixed ? kMixedRel : 0.0, val, vis, I2, p2, q2, done2, res2);
+        if constexpr (kMixed) {
+          auto val = [&](int t) {
+            const ff *e = (const ff *)(tab + (t - s0) * TSf);
+            return ff_mul(e[lq + l1], e[l2]);
+          };
+          psm92_advance_ff(s0, s1, J.tol, val, vis, I2, p2, q2, done2, res2);
+        } else {
+          auto val = [&](int t) {
+            const double *e = tab + (t - s0) * TSf;
+            return e[lq + l1] * e[l2];
+          };
+          psm92_advance(s0, s1, J.tol, val, vis, I2, p2, q2, done2, res2);
+        }
       }
       __syncwarp();
       s0 = s1;
@@ -910,6 +1072,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
   // zeta_b^max(0, shiftb) (src/type2.c:456-462)
   const double Ck = zeta_times(zeta_times(ca * cb, za, pa0), zb, pb0);
   const double i1 = map[2 * k], i2 = map[2 * k + 1];
+  const ff i1f = ff_from_double(i1), Ckf = ff_from_double(Ck);
   const int nb = S.ppBreak[k], end = nb == INT_MAX ? OL - 1 : nb - 1;
   const int nLo = win[2 * k], nHi = win[2 * k + 1];
   // the latest break of the earlier pairs: beyond it no earlier pair's
@@ -994,18 +1157,33 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       locate(t, owner, r, ex);
       const double zaj = pzA[owner / Nb], zbj = pzB[owner % Nb];
       double *e = tab + lane * TS;
-      double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
-      // Ka rows carry the weight and prefactor: w * Ck * e^(..) * K_l1
-      const double wB = (J.wLarge[n] * i1) * (Ck * fast_exp(ex));
-      // only the channels and rows this pass's quadratures read
-      channels_masked<kMixed>(J, c, r, pMask, U);
-      // the rows of both centres through one copy of the Bessel code
+      if constexpr (kMixed) {
+        // the same rows in double-single
+        ff *U = (ff *)(e + 3), *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
+        const ff rf = ff_from_double(r);
+        const ff wB = ff_mul(ff_mul(J.wLf[n], i1f), ff_mul(Ckf, ff_exp(ff_from_double(ex))));
+        channels_ff(J, c, rf, pMask, U);
 #pragma unroll 1
-      for (int side = 0; side < 2; side++)
-        bessel_fast<kMixed>(J, side ? pL2 : pL1, side ? 2.0 * zbj * dBC * r : 2.0 * zaj * dAC * r, side ? Kb : Ka, 1);
-      for (int l = 0; l <= pL1; l++) Ka[l] *= wB;
-      R[0] = 1.0;
-      for (int l = 1; l <= pL3; l++) R[l] = r * R[l - 1];
+        for (int side = 0; side < 2; side++)
+          bessel_ff(J, side ? pL2 : pL1, ff_mul(ff_from_double(side ? 2.0 * zbj * dBC : 2.0 * zaj * dAC), rf),
+                    side ? Kb : Ka, 1);
+        for (int l = 0; l <= pL1; l++) Ka[l] = ff_mul(Ka[l], wB);
+        R[0] = {1.0f, 0.0f};
+        for (int l = 1; l <= pL3; l++) R[l] = ff_mul(rf, R[l - 1]);
+      } else {
+        double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
+        // Ka rows carry the weight and prefactor: w * Ck * e^(..) * K_l1
+        const double wB = (J.wLarge[n] * i1) * (Ck * fast_exp(ex));
+        // only the channels and rows this pass's quadratures read
+        channels_masked<kMixed>(J, c, r, pMask, U);
+        // the rows of both centres through one copy of the Bessel code
+#pragma unroll 1
+        for (int side = 0; side < 2; side++)
+          bessel_fast<kMixed>(J, side ? pL2 : pL1, side ? 2.0 * zbj * dBC * r : 2.0 * zaj * dAC * r, side ? Kb : Ka, 1);
+        for (int l = 0; l <= pL1; l++) Ka[l] *= wB;
+        R[0] = 1.0;
+        for (int l = 1; l <= pL3; l++) R[l] = r * R[l - 1];
+      }
     }
     if (lane == 0) {  // entry of slot t: queued slots in [wpos, t)
       const int w0 = wpos >> 5, w1 = (b - 1) >> 5;
@@ -1025,16 +1203,27 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       while (qq >= J.itemCnt[ncls + l]) { qq -= J.itemCnt[ncls + l]; l++; }
       int it = J.items[J.itemOff[ncls + l] + qq];
       int l1 = it & 255, l2 = (it >> 8) & 255, l3 = it >> 16;
-      auto val = [&](int t) {  // a queued slot
+      auto entry = [&](int t) {  // a queued slot's table entry
         const unsigned word = needBits[t >> 5], bit = 1u << (t & 31);
-        const double *e = tab + (pref[t >> 5] + __popc(word & (bit - 1u))) * TS;
-        const double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
-        return Ka[l1] * Kb[l2] * U[l] * R[l3];
+        return tab + (pref[t >> 5] + __popc(word & (bit - 1u))) * TS;
       };
       auto vis = [&](int t) { return c92_slot[t] <= end; };  // an upper slot
       double I = sI[q], p = sP[q], qv = sQ[q], res = 0;
       bool done = false;
-      psm92_sparse(wpos, b, needBits, J.tol, kMixed ? kMixedRel : 0.0, val, vis, I, p, qv, done, res);
+      if constexpr (kMixed) {
+        auto val = [&](int t) {
+          const ff *U = (const ff *)(entry(t) + 3), *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
+          return ff_mul(ff_mul(ff_mul(Ka[l1], Kb[l2]), U[l]), R[l3]);
+        };
+        psm92_sparse_ff(wpos, b, needBits, J.tol, val, vis, I, p, qv, done, res);
+      } else {
+        auto val = [&](int t) {
+          const double *e = entry(t);
+          const double *U = e + 3, *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
+          return Ka[l1] * Kb[l2] * U[l] * R[l3];
+        };
+        psm92_sparse(wpos, b, needBits, J.tol, val, vis, I, p, qv, done, res);
+      }
       sI[q] = I; sP[q] = p; sQ[q] = qv;
       if (done) { sR[q] = res; doneBits[qi] |= 1u << lane; }
       else {

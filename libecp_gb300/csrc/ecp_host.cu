@@ -214,7 +214,7 @@ int parse_system(const ecpgb_system &s, Parsed &P) {
 struct DevTables {
   TableKey key{};
   HostTables host;
-  DBuf<float> besHf;
+  DBuf<float> besHf, besAf, besZf, xlf, wlf;  // float pairs (mixed path)
   DBuf<double> xs, ws, xl, wl, besT, besC, besH, besA, besZ, shNorm, p2s, fac, dfac, omega, c2s;
   DBuf<int> ijk, ijkIdx, itemOff, itemCnt, items, s93, s92;
   DBuf<short> byN93;
@@ -294,6 +294,8 @@ struct Engine {
               t->fac.upload(h.fac, stream) && t->dfac.upload(h.dfac, stream) &&
               t->omega.upload(h.omega, stream) && t->ijk.upload(h.ijk, stream) &&
               t->ijkIdx.upload(h.ijkIndex, stream) && t->besH.upload(h.besselH, stream) && t->besA.upload(h.besselA, stream) && t->besHf.upload(h.besselHf, stream) &&
+              t->besAf.upload(h.besselAf, stream) && t->besZf.upload(h.besselZf, stream) &&
+              t->xlf.upload(h.xlf, stream) && t->wlf.upload(h.wlf, stream) &&
               t->besZ.upload(h.besselZ, stream) &&
               t->c2s.upload(h.cart2sph, stream) && t->s93.upload(h.s93.slot, stream) &&
               t->s92.upload(h.s92.slot, stream) && t->byN93.upload(by_point_order(h.s93.slot), stream) &&
@@ -446,7 +448,8 @@ size_t job_device_bytes(const Parsed &P, int mode) {
   const size_t angLam = P.maxLECP + LB + 1, angC = (LB + 1) * (LB + 2) * (LB + 3) / 6;
   size_t in = 8 * (P.geom.size() + P.primA.size() + P.primD.size() + 3 * P.termL.size() + P.pairOff.size()) +
               4 * (5 * P.shL.size() + P.atomMaxL.size() + 4 * P.ctrAtom.size() + P.termL.size() + 3 * P.pairA.size()) +
-              (mode != ECPGB_FP64 ? 4 * nc * P.nPairs : 0) + 21 * 256;
+              (mode != ECPGB_FP64 ? 4 * nc * P.nPairs : 0) + (mode == ECPGB_MIXED ? 16 * P.termL.size() : 0) +
+              23 * 256;
   size_t work = 8 * (ns + nc * O * LE * nk + nc * O + nc * ns * (1 + P.deriv) * O * nF + nc * na * 4 + nc * na * D * D * D +
                      nc * na * angLam * LE * LE * angC + nc * (size_t)P.centreStride + (size_t)P.dim * P.dim) +
                 4 * (nc + nc * ns * 3 + nc * (size_t)P.nPairs + 2) + 8;
@@ -493,6 +496,13 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   std::vector<int> order;
   if (mode != ECPGB_FP64) unit_order(P, order);
   size_t iOrd = add(order.data(), 4 * order.size());
+  // the ECP terms' exponents and coefficients as float pairs (mixed path)
+  std::vector<float> tAf, tDf;
+  if (mode == ECPGB_MIXED) {
+    split_pairs(P.termA, tAf);
+    split_pairs(P.termD, tDf);
+  }
+  size_t iTAf = add(tAf.data(), 4 * tAf.size()), iTDf = add(tDf.data(), 4 * tDf.size());
   if (!B.pinned.ensure(tot) || !B.in.ensure(tot)) {
     set_error("allocation of %zu input bytes failed", tot);
     return -1;
@@ -510,6 +520,8 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.ctrNT = (const int *)dp(iCN); J.termL = (const int *)dp(iTL); J.pairA = (const int *)dp(iPrA);
   J.pairB = (const int *)dp(iPrB); J.pairOff = (const long long *)dp(iPO);
   J.pairShift = (const int *)dp(iPS);
+  J.termAf = mode == ECPGB_MIXED ? (const ff *)dp(iTAf) : nullptr;
+  J.termDf = mode == ECPGB_MIXED ? (const ff *)dp(iTDf) : nullptr;
   J.deriv = P.deriv;
   J.nRuns = 1 + P.deriv;
   J.order = order.empty() ? nullptr : (const int *)dp(iOrd);
@@ -548,7 +560,11 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.besH = T->besH.p;
   J.besA = T->besA.p;
   J.besZ = T->besZ.p;
-  J.besHf = T->besHf.p;
+  J.besHf = (const ff *)T->besHf.p;
+  J.besAf = (const ff *)T->besAf.p;
+  J.besZf = (const ff *)T->besZf.p;
+  J.xLf = (const ff *)T->xlf.p;
+  J.wLf = (const ff *)T->wlf.p;
   J.s93 = T->s93.p;
   J.s92 = T->s92.p;
   J.byN93 = T->byN93.p;

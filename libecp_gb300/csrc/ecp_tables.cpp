@@ -9,6 +9,7 @@
 #include <cstdlib>
 
 namespace ecpgb {
+void split_pairs(const std::vector<double> &d, std::vector<float> &out);
 
 static const double kPi = 3.14159265358979323846;
 
@@ -379,6 +380,8 @@ void build_tables(const TableKey &key, HostTables &t) {
   grid_ps93(128, t.xs, t.ws);
   schedule_ps93(128, t.s93);
   grid_psm92(key.largeGridOrder, t.xl, t.wl);
+  split_pairs(t.xl, t.xlf);
+  split_pairs(t.wl, t.wlf);
   schedule_psm92((int)t.xl.size(), t.s92);
   t.tabL = t.maxLECP + t.maxAlpha + 6;
   if (t.tabL < 2 * t.maxLBS + 5) t.tabL = 2 * t.maxLBS + 5;
@@ -395,6 +398,17 @@ void build_tables(const TableKey &key, HostTables &t) {
     double norm0 = std::sqrt((2.0 * l + 1.0) / (2.0 * kPi));
     t.shNorm[(size_t)l * W] = norm0;
     for (int m = 1; m <= l; m++) t.shNorm[(size_t)l * W + m] = std::sqrt(t.fac[l - m] / t.fac[l + m]) * norm0;
+  }
+}
+
+// Doubles as float pairs (hi = nearest float, lo = nearest float to the
+// remainder), interleaved: the layout of the mixed path's ff values.
+void split_pairs(const std::vector<double> &d, std::vector<float> &out) {
+  out.resize(2 * d.size());
+  for (size_t i = 0; i < d.size(); i++) {
+    const float hi = (float)d[i];
+    out[2 * i] = hi;
+    out[2 * i + 1] = std::isfinite(hi) ? (float)(d[i] - (double)hi) : 0.0f;
   }
 }
 
@@ -419,7 +433,6 @@ void bessel_horner(HostTables &t) {
       for (int l = 0; l <= HL; l++) c[l * 6 + k] = d[l] * invfact[k];
     }
   }
-  t.besselHf.assign(t.besselH.begin(), t.besselH.end());
   const double h = t.besselN / 16;  // integer division, as src/bessel.c:138-143
   t.besselZ.resize(N);
   for (int i = 0; i < N; i++) t.besselZ[i] = i / h;
@@ -434,6 +447,9 @@ void bessel_horner(HostTables &t) {
       f *= (double)(l + i + 1) * (l - i);
     }
   }
+  split_pairs(t.besselH, t.besselHf);
+  split_pairs(t.besselA, t.besselAf);
+  split_pairs(t.besselZ, t.besselZf);
 }
 
 void used_triples(int la, int lb, int l, std::vector<int> &out) {

@@ -80,7 +80,9 @@ struct HostTables {
   // max(besselHL + 1, 6), zero beyond i = l.  The coefficients are the integers (l+i)!/((l-i)! i!), the
   // reference's running product divided by i!, so they are exact in FP64.
   std::vector<double> besselA;
-  std::vector<float> besselHf;   // besselH rounded to FP32 (mixed-precision mode)
+  // mixed-precision path: the tables above split into float pairs (hi, lo)
+  // with hi + lo = the double to 48 bits (ecp_ff.h), interleaved
+  std::vector<float> besselHf, besselAf, besselZf, xlf, wlf;
   std::vector<double> besselZ;   // table abscissae z_i = i / (besselN / 16), the reference's division
   // Normalisation of the real spherical harmonics, [l][m] for l, m <= tmDim:
   // sqrt((2l+1)/(2 pi)) and sqrt((l-m)!/(l+m)!) times that, computed as
@@ -94,6 +96,7 @@ struct HostTables {
 // Builds every table for the key.  status != 0 reports a failure.
 void build_tables(const TableKey &key, HostTables &t);
 void bessel_horner(HostTables &t);
+void split_pairs(const std::vector<double> &d, std::vector<float> &out);
 
 // Used triples (l1, l2, l3) of the type-2 radial table for one (la, lb, l):
 // exactly those the angular linking of calcGamma (src/type2.c:583-623) reads.
