@@ -142,7 +142,9 @@ void ecpgb_job_free(ecpgb_job *j);
 /* Launch configuration of the batched path (ECPGB_FAST).  queue: 1 = a
  * persistent launch whose CTAs pull units from a work queue, 0 = one CTA per
  * unit; sorted: 1 = the queue holds the units by descending estimated cost
- * (primitive pairs x (la + lb + 2) x (L + 2)), 0 = the reference's order;
+ * (primitive pairs x (la + lb + 2) x (L + 2)), 2 = grouped by (la, lb, L)
+ * class (largest la + lb first), by that cost within a class, 0 = the
+ * reference's order;
  * gcap: width cap of the type-1 step table in doubles per slot, which sets
  * the primitive pairs per warp and the CTAs per SM; balance: 1 = a unit with
  * few primitive pairs gets narrower type-1 groups so that all its warps

@@ -98,6 +98,7 @@ struct DevJob {
   int *errWord;          // [0] first unit with a warning (atomicMin), [1] input error flags
   // batched path: work queue and tuning
   const int *order;              // units by descending estimated cost (null: natural order)
+  const int *orderClass;         // units grouped by (la, lb, L) class, by cost within a class
   unsigned long long *queueHead; // next queue position (persistent launch); reset per run
   int gcap;                      // type-1 step-table width cap (doubles per slot per warp)
   int maxNP;                     // most primitive pairs of a shell pair (shared-memory sizing)
@@ -112,7 +113,7 @@ struct DevJob {
 // Launch configuration of the batched path (picked by the autotuner).
 struct FastConfig {
   int queue = 1;   // 1: persistent CTAs pulling units from the work queue; 0: a CTA per unit
-  int sorted = 1;  // 1: units by descending estimated cost; 0: the reference's order
+  int sorted = 1;  // 1: units by descending estimated cost; 2: class-major; 0: the reference's order
   int gcap = 45;   // type-1 step-table width cap; smaller caps fit more CTAs per SM
   int mixed = 0;   // set from the job's mode (ECPGB_MIXED), not tuned
   int balance = 1; // narrower type-1 groups when a unit has few primitive pairs

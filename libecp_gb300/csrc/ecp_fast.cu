@@ -64,7 +64,7 @@ static __device__ void bessel_small(int lmax, double z, double *K, int stride) {
 }
 
 template <bool kMixed>
-static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *K, int stride) {
+static __device__ __noinline__ void bessel_fast(const DevJob &J, int lmax, double z, double *K, int stride) {
   if (__builtin_expect(z < 1.0E-7, 0)) {  // rare: laid out of line
     bessel_small(lmax, z, K, stride);
     return;
@@ -104,7 +104,7 @@ static __device__ void bessel_fast(const DevJob &J, int lmax, double z, double *
 }
 
 // One row K_l(z), by the same branches as bessel_fast.
-static __device__ double bessel_row(const DevJob &J, int l, double z) {
+static __device__ __noinline__ double bessel_row(const DevJob &J, int l, double z) {
   if (__builtin_expect(z < 1.0E-7, 0)) {  // rare: laid out of line
     if (z <= 0) return l == 0 ? 1.0 : 0.0;
     double v = 1 - z;
@@ -137,7 +137,7 @@ static __device__ double bessel_row(const DevJob &J, int l, double z) {
 // U_l(r) of centre c for the channels l set in mask, in one pass over its
 // terms (src/ecp.c:42-60); the other entries of U are left untouched.
 template <bool kMixed>
-static __device__ void channels_masked(const DevJob &J, int c, double r, unsigned mask, double *U) {
+static __device__ __noinline__ void channels_masked(const DevJob &J, int c, double r, unsigned mask, double *U) {
   double r2 = r * r;
   for (unsigned m = mask; m; m &= m - 1) U[__ffs(m) - 1] = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
@@ -148,7 +148,7 @@ static __device__ void channels_masked(const DevJob &J, int c, double r, unsigne
 }
 
 template <bool kMixed>
-static __device__ double channel(const DevJob &J, int c, int l, double r) {
+static __device__ __noinline__ double channel(const DevJob &J, int c, int l, double r) {
   double r2 = r * r, pot = 0.0;
   int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
   for (int t = t0; t < t1; t++)
@@ -179,7 +179,7 @@ static __device__ inline ff ff_recip(ff z) {
 
 // K_0..K_lmax(z) in ff: the branches of bessel_fast over the tables' float
 // pairs (Taylor coefficients, table abscissae, large-argument polynomial).
-static __device__ void bessel_ff(const DevJob &J, int lmax, ff z, ff *K, int stride) {
+static __device__ __noinline__ void bessel_ff(const DevJob &J, int lmax, ff z, ff *K, int stride) {
   if (__builtin_expect(z.hi < 1.0e-7f, 0)) {  // rare: the small-argument formula in FP64
     double Kd[kMaxRows];
     bessel_small(lmax, ff_to_double(z), Kd, 1);
@@ -232,7 +232,7 @@ static __device__ inline ff ecp_term_ff(const DevJob &J, int t, ff r, ff r2) {
 }
 
 // U_l(r) in ff for the channels set in mask (the others untouched).
-static __device__ void channels_ff(const DevJob &J, int c, ff r, unsigned mask, ff *U) {
+static __device__ __noinline__ void channels_ff(const DevJob &J, int c, ff r, unsigned mask, ff *U) {
   const ff r2 = ff_mul(r, r);
   for (unsigned m = mask; m; m &= m - 1) U[__ffs(m) - 1] = {0.0f, 0.0f};
   const int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
@@ -242,7 +242,7 @@ static __device__ void channels_ff(const DevJob &J, int c, ff r, unsigned mask, 
   }
 }
 
-static __device__ ff channel_ff(const DevJob &J, int c, int l, ff r) {
+static __device__ __noinline__ ff channel_ff(const DevJob &J, int c, int l, ff r) {
   const ff r2 = ff_mul(r, r);
   ff pot = {0.0f, 0.0f};
   const int t0 = J.ctrT0[c], t1 = t0 + J.ctrNT[c];
@@ -283,7 +283,7 @@ static __device__ inline double t1_exponent(double z, double s, double r) {
 // integrand that is 0 except NaN at window points whose exp(e) overflows:
 // the first level that counts a point converges to 0 unless a NaN has been
 // summed by then, after which no level converges.
-static __device__ bool t1_zero_walk(const DevJob &J, double s, double z, int ws, int we) {
+static __device__ __noinline__ bool t1_zero_walk(const DevJob &J, double s, double z, int ws, int we) {
   auto nan_at = [&](int n) {
     if (n < ws || n >= we) return false;
     const double e = t1_exponent(z, s, J.xSmall[n]);
@@ -1811,6 +1811,7 @@ int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, con
   Jc.mixed = cfg.mixed;
   Jc.balance = cfg.balance;
   if (!cfg.sorted) Jc.order = nullptr;
+  else if (cfg.sorted == 2 && J.orderClass) Jc.order = J.orderClass;
   const bool screen = cfg.queue && cfg.screen && J.queueHead && J.live && J.liveCount && J.screenBlocks;
   if (!screen) Jc.live = nullptr;
   launch_prologue(Jc, st, false);

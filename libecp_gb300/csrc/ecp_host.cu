@@ -405,6 +405,28 @@ static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 
 bool valid_mode(int mode) { return mode == ECPGB_FP64 || mode == ECPGB_FAST || mode == ECPGB_MIXED; }
 
+// The class-major work queue: units grouped by their (la, lb, L) class --
+// largest la + lb first, then la, then the centre's L descending -- and
+// within a class by descending estimated cost, ties in the reference's order.
+// Concurrent CTAs then mostly run units of one class, i.e. the same code
+// paths and table widths.  Empty when the units do not fit 31-bit indices.
+static void unit_order_class(const Parsed &P, std::vector<int> &order) {
+  order.clear();
+  const long long n = (long long)P.nCentres * P.nPairs;
+  if (n <= 0 || n >= INT_MAX) return;
+  std::vector<long long> key(n);
+  for (int c = 0; c < P.nCentres; c++)
+    for (int p = 0; p < P.nPairs; p++) {
+      const int a = P.pairA[p], b = P.pairB[p], la = P.shL[a], lb = P.shL[b], L = P.ctrL[c];
+      const long long cls = ((long long)(64 - la - lb) * 64 + (64 - la)) * 64 + (64 - L);
+      const long long cost = (long long)P.shK[a] * P.shK[b] * (la + lb + 2) * (L + 2);
+      key[(size_t)c * P.nPairs + p] = cls * (1LL << 32) + ((1LL << 31) - 1 - cost);
+    }
+  order.resize(n);
+  for (long long u = 0; u < n; u++) order[u] = (int)u;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
+}
+
 // The work queue of the batched path: units by descending estimated cost,
 // primitive pairs x (la + lb + 2) x (L + 2), ties in the reference's order
 // (a stable counting sort).  Empty when the units do not fit 31-bit indices.
@@ -448,8 +470,8 @@ size_t job_device_bytes(const Parsed &P, int mode) {
   const size_t angLam = P.maxLECP + LB + 1, angC = (LB + 1) * (LB + 2) * (LB + 3) / 6;
   size_t in = 8 * (P.geom.size() + P.primA.size() + P.primD.size() + 3 * P.termL.size() + P.pairOff.size()) +
               4 * (5 * P.shL.size() + P.atomMaxL.size() + 4 * P.ctrAtom.size() + P.termL.size() + 3 * P.pairA.size()) +
-              (mode != ECPGB_FP64 ? 4 * nc * P.nPairs : 0) + (mode == ECPGB_MIXED ? 16 * P.termL.size() : 0) +
-              23 * 256;
+              (mode != ECPGB_FP64 ? 8 * nc * P.nPairs : 0) + (mode == ECPGB_MIXED ? 16 * P.termL.size() : 0) +
+              24 * 256;
   size_t work = 8 * (ns + nc * O * LE * nk + nc * O + nc * ns * (1 + P.deriv) * O * nF + nc * na * 4 + nc * na * D * D * D +
                      nc * na * angLam * LE * LE * angC + nc * (size_t)P.centreStride + (size_t)P.dim * P.dim) +
                 4 * (nc + nc * ns * 3 + nc * (size_t)P.nPairs + 2) + 8;
@@ -493,9 +515,12 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
          iTL = add(P.termL.data(), 4 * P.termL.size()), iPrA = add(P.pairA.data(), 4 * P.pairA.size()),
          iPrB = add(P.pairB.data(), 4 * P.pairB.size()), iPO = add(P.pairOff.data(), 8 * P.pairOff.size()),
          iPS = add(P.pairShift.data(), 4 * P.pairShift.size());
-  std::vector<int> order;
-  if (mode != ECPGB_FP64) unit_order(P, order);
-  size_t iOrd = add(order.data(), 4 * order.size());
+  std::vector<int> order, orderClass;
+  if (mode != ECPGB_FP64) {
+    unit_order(P, order);
+    unit_order_class(P, orderClass);
+  }
+  size_t iOrd = add(order.data(), 4 * order.size()), iOrdC = add(orderClass.data(), 4 * orderClass.size());
   // the ECP terms' exponents and coefficients as float pairs (mixed path)
   std::vector<float> tAf, tDf;
   if (mode == ECPGB_MIXED) {
@@ -525,6 +550,7 @@ int stage_job(const Parsed &P, const DevTables *T, JobBuffers &B, DevJob &J, int
   J.deriv = P.deriv;
   J.nRuns = 1 + P.deriv;
   J.order = order.empty() ? nullptr : (const int *)dp(iOrd);
+  J.orderClass = orderClass.empty() ? nullptr : (const int *)dp(iOrdC);
   J.centreStride = P.centreStride;
   // --- tables
   J.itemOff = T->itemOff.p; J.itemCnt = T->itemCnt.p; J.items = T->items.p;
@@ -991,6 +1017,8 @@ int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials,
     for (int queue : {1, 0}) cand.push_back(mk(queue, 1, gcap, 1));
   cand.push_back(mk(0, 0, 45, 1));
   cand.push_back(mk(1, 1, 45, 0));
+  for (int gcap : {45, 64}) cand.push_back(mk(1, 2, gcap, 1));
+  cand.push_back(mk(1, 2, 45, 0));
   FastConfig noScreen = mk(1, 1, 45, 1);
   noScreen.screen = 0;
   cand.push_back(noScreen);
@@ -1043,7 +1071,7 @@ int job_config(void *vj, const ecpgb_launch_config *cfg, ecpgb_launch_config *ou
     if (cfg->gcap < 1 || cfg->gcap > 4096) { set_error("gcap %d out of range", cfg->gcap); return 1; }
     FastConfig c;
     c.queue = cfg->queue ? 1 : 0;
-    c.sorted = cfg->sorted ? 1 : 0;
+    c.sorted = cfg->sorted == 2 ? 2 : (cfg->sorted ? 1 : 0);
     c.gcap = cfg->gcap;
     c.balance = cfg->balance ? 1 : 0;
     c.screen = cfg->screen ? 1 : 0;
