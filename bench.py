@@ -277,6 +277,9 @@ def ours(args, rank, world):
     serving = None
     if rank == 0 and args.serve_seconds > 0 and mode == eg.ECPGB_FAST:
         serving = serving_run(eg, args.serve_rate, args.serve_seconds)
+        if args.serve_mixed_seconds > 0:
+            serving = {"batched_fp64": serving,
+                       "mixed": serving_run(eg, args.serve_rate, args.serve_mixed_seconds, eg.ECPGB_MIXED)}
 
     mixed = None
     if rank == 0 and args.mixed_report and mode != eg.ECPGB_FP64:
@@ -378,21 +381,25 @@ def ours(args, rank, world):
     return line
 
 
-def serving_run(eg, rate, seconds):
+def serving_run(eg, rate, seconds, mode=None, slots=32):
     """The serving stream (molecules of 5-200 atoms, 1-40 ECP centres, s..f
     shells of 1-6 primitives) at `rate` requests/s for `seconds` through the
     request server; latency percentiles as the server measured them."""
     from libecp_gb300 import serve
+    mode = eg.ECPGB_FAST if mode is None else mode
     arrivals = serve.poisson_arrivals(rate, seconds, seed=7)
     systems = serve.request_stream(len(arrivals), seed=7)
-    with eg.Server(mode=eg.ECPGB_FAST, budget_bytes=64 << 30, slots=8) as sv:
+    with eg.Server(mode=mode, budget_bytes=64 << 30, slots=slots) as sv:
         r = serve.run_stream(sv, systems, arrivals)
-    return {"stream": "Poisson; 5-200 atoms (log-uniform), 1-40 ECP centres, s..f shells of 1-6 primitives",
+    return {"path": "batched FP64" if mode == eg.ECPGB_FAST else "mixed precision",
+            "stream": "Poisson; 5-200 atoms (log-uniform), 1-40 ECP centres, s..f shells of 1-6 primitives",
             "offered_rate_per_s": rate, "seconds": seconds, "requests": r["requests"],
             "errors": len(r["errors"]), "served_rate_per_s": r["served_rate"],
             "units_per_s": r["units_per_s"], "latency_ms": r["latency_ms"], "queued_ms": r["queued_ms"],
-            "gpu_ms": r["gpu_ms"], "hbm_budget_bytes": 64 << 30, "slots": 8,
-            "max_inflight": r["stats"]["maxInflight"]}
+            "gpu_ms": r["gpu_ms"], "hbm_budget_bytes": 64 << 30, "slots": slots,
+            "max_inflight": r["stats"]["maxInflight"],
+            "batching": "continuous: jobs overlap on per-slot streams; each CTA takes at most 8 units, "
+                        "jobs under 100k units on high-priority streams"}
 
 
 def reference_arm(args, rank, world):
@@ -429,10 +436,13 @@ def main():
                     help="batched: the fast FP64 path; fp64: the plain drop-in kernels")
     ap.add_argument("--compare-plain", type=int, default=1,
                     help="also time the plain FP64 path (2 steps) for the ratio")
-    ap.add_argument("--serve-rate", type=float, default=1.5,
-                    help="serving stream arrival rate (requests/s)")
-    ap.add_argument("--serve-seconds", type=float, default=20.0,
-                    help="serving stream length (0: no serving run)")
+    ap.add_argument("--serve-rate", type=float, default=3.0,
+                    help="serving stream arrival rate (requests/s; one GB300 serves about 3.5 of this "
+                         "stream's requests per second)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="serving stream length on the batched FP64 path (0: no serving run)")
+    ap.add_argument("--serve-mixed-seconds", type=float, default=30.0,
+                    help="serving stream length on the mixed-precision path (0: none)")
     ap.add_argument("--workload", default="cluster", choices=list(WORKLOADS),
                     help="cluster (the headline), cluster8 (its first 8 centres: profiler captures), "
                          "mixed_batch and sweep (the other configurations)")

@@ -104,6 +104,7 @@ struct DevJob {
   int maxNP;                     // most primitive pairs of a shell pair (shared-memory sizing)
   int mixed;                     // 1: the fallbacks' tables and sums in double-single (ecp_ff.h)
   int balance;                   // 1: type-1 groups narrowed so that every warp gets pairs
+  int ctaUnits;                  // >0: a persistent CTA takes at most this many units, then exits
   // screening stage (batched path): the queue of units that compute blocks
   int *live;                     // live units in queue order (null: no screening stage)
   unsigned long long *liveCount; // their number

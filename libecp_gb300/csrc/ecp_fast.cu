@@ -1673,7 +1673,9 @@ __global__ void __launch_bounds__(kUnitThreads, kUnitCtasPerSm) k_unit_queue(Dev
   __shared__ long long next;
   // with the screening stage the queue holds the live units only
   const long long n = J.live ? (long long)*J.liveCount : (long long)J.nCentres * J.nPairs;
-  for (;;) {
+  // ctaUnits > 0: a CTA takes at most that many units and exits, so that
+  // the SMs free up for other launches (the request server's jobs)
+  for (int taken = 0; J.ctaUnits <= 0 || taken < J.ctaUnits; taken++) {
     if (threadIdx.x == 0) next = (long long)atomicAdd(J.queueHead, 1ull);
     __syncthreads();
     const long long i = next;
@@ -1835,6 +1837,11 @@ int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, con
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       int per = fast_ctas_per_sm(smemBytes, 1);
       long long grid = (long long)sms * (per > 0 ? per : 1);
+      if (J.ctaUnits > 0) {  // bounded CTAs: enough of them for every unit
+        const long long need = (nUnits + J.ctaUnits - 1) / J.ctaUnits;
+        grid = need > grid ? need : grid;
+        if (grid > (1LL << 30)) grid = 1LL << 30;
+      }
       if (grid > nUnits) grid = nUnits;
       if (cfg.mixed) k_unit_queue<true><<<(unsigned)grid, kUnitThreads, smemBytes, st>>>(Jc);
       else k_unit_queue<false><<<(unsigned)grid, kUnitThreads, smemBytes, st>>>(Jc);

@@ -403,6 +403,26 @@ void wait_schedules_unpinned(std::unique_lock<std::mutex> &lk) {
 
 static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 
+cudaStream_t &alloc_stream() {
+  static thread_local cudaStream_t s = nullptr;
+  return s;
+}
+
+static std::mutex g_retiredMu;
+std::vector<void *> &retired_pinned() {
+  static std::vector<void *> v;
+  return v;
+}
+void retire_pinned(void *p) {
+  std::lock_guard<std::mutex> lk(g_retiredMu);
+  retired_pinned().push_back(p);
+}
+void free_retired_pinned() {
+  std::lock_guard<std::mutex> lk(g_retiredMu);
+  for (void *p : retired_pinned()) cudaFreeHost(p);
+  retired_pinned().clear();
+}
+
 bool valid_mode(int mode) { return mode == ECPGB_FP64 || mode == ECPGB_FAST || mode == ECPGB_MIXED; }
 
 // The class-major work queue: units grouped by their (la, lb, L) class --
@@ -414,17 +434,40 @@ static void unit_order_class(const Parsed &P, std::vector<int> &order) {
   order.clear();
   const long long n = (long long)P.nCentres * P.nPairs;
   if (n <= 0 || n >= INT_MAX) return;
-  std::vector<long long> key(n);
+  // two stable counting sorts (least significant key first): by descending
+  // cost, then by class
+  std::vector<int> pc(P.nPairs), cc(P.nCentres), pcls(P.nPairs);
+  int maxP = 0, maxC = 0, LB = 0, LE = 0;
+  for (int c = 0; c < P.nCentres; c++) { cc[c] = P.ctrL[c] + 2; maxC = std::max(maxC, cc[c]); LE = std::max(LE, P.ctrL[c]); }
+  for (int p = 0; p < P.nPairs; p++) {
+    const int a = P.pairA[p], b = P.pairB[p];
+    pc[p] = P.shK[a] * P.shK[b] * (P.shL[a] + P.shL[b] + 2);
+    maxP = std::max(maxP, pc[p]);
+    LB = std::max(LB, std::max(P.shL[a], P.shL[b]));
+  }
+  const long long nCost = (long long)maxP * maxC + 1;
+  if (nCost > (1 << 24)) return;
+  const int W1 = LB + 1, W2 = LE + 1, nCls = (2 * LB + 1) * W1 * W2;
+  for (int p = 0; p < P.nPairs; p++) {
+    const int la = P.shL[P.pairA[p]], lb = P.shL[P.pairB[p]];
+    pcls[p] = ((2 * LB - la - lb) * W1 + (LB - la)) * W2;  // + (LE - L) per centre
+  }
+  std::vector<int> tmp(n);
+  std::vector<int> start(std::max<long long>(nCost, nCls) + 1);
+  // pass 1: by descending cost, ties in the reference's order
+  std::fill(start.begin(), start.begin() + nCost + 1, 0);
   for (int c = 0; c < P.nCentres; c++)
-    for (int p = 0; p < P.nPairs; p++) {
-      const int a = P.pairA[p], b = P.pairB[p], la = P.shL[a], lb = P.shL[b], L = P.ctrL[c];
-      const long long cls = ((long long)(64 - la - lb) * 64 + (64 - la)) * 64 + (64 - L);
-      const long long cost = (long long)P.shK[a] * P.shK[b] * (la + lb + 2) * (L + 2);
-      key[(size_t)c * P.nPairs + p] = cls * (1LL << 32) + ((1LL << 31) - 1 - cost);
-    }
+    for (int p = 0; p < P.nPairs; p++) start[nCost - 1 - (long long)pc[p] * cc[c]]++;
+  for (long long k = 0, acc = 0; k <= nCost; k++) { const int v = start[k]; start[k] = (int)acc; acc += v; }
+  for (int c = 0; c < P.nCentres; c++)
+    for (int p = 0; p < P.nPairs; p++) tmp[start[nCost - 1 - (long long)pc[p] * cc[c]]++] = c * P.nPairs + p;
+  // pass 2: by class, stable
+  auto cls = [&](int u) { const int c = u / P.nPairs; return pcls[u % P.nPairs] + (LE - P.ctrL[c]); };
+  std::fill(start.begin(), start.begin() + nCls + 1, 0);
+  for (long long i = 0; i < n; i++) start[cls(tmp[i])]++;
+  for (int k = 0, acc = 0; k <= nCls; k++) { const int v = start[k]; start[k] = acc; acc += v; }
   order.resize(n);
-  for (long long u = 0; u < n; u++) order[u] = (int)u;
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
+  for (long long i = 0; i < n; i++) order[start[cls(tmp[i])]++] = tmp[i];
 }
 
 // The work queue of the batched path: units by descending estimated cost,

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "ecp_engine.h"
@@ -44,6 +45,11 @@ void shift_block_l(int deriv, int la, int lb, int shifta, int shiftb, int &lpa, 
 struct TableKey;
 TableKey table_key(const Parsed &P);
 
+// The stream on which the calling thread's buffer growth is ordered: with a
+// stream set, DBuf grows with cudaFreeAsync / cudaMallocAsync on it, which
+// do not wait for the rest of the device (cudaFree does); null: cudaMalloc.
+cudaStream_t &alloc_stream();
+
 // Grow-only device buffer.
 template <class T>
 struct DBuf {
@@ -51,12 +57,27 @@ struct DBuf {
   size_t cap = 0;
   bool ensure(size_t n) {
     if (n <= cap) return true;
-    if (p) cudaFree(p);
+    cudaStream_t s = alloc_stream();
+    if (p) {
+      if (s) cudaFreeAsync(p, s);
+      else cudaFree(p);
+    }
     p = nullptr;
     cap = 0;
-    if (cudaMalloc((void **)&p, n * sizeof(T)) != cudaSuccess) return false;
+    if ((s ? cudaMallocAsync((void **)&p, n * sizeof(T), s) : cudaMalloc((void **)&p, n * sizeof(T))) !=
+        cudaSuccess)
+      return false;
     cap = n;
     return true;
+  }
+  // Releases the memory, ordered on stream s (null: cudaFree).
+  void release(cudaStream_t s) {
+    if (p) {
+      if (s) cudaFreeAsync(p, s);
+      else cudaFree(p);
+    }
+    p = nullptr;
+    cap = 0;
   }
   bool upload(const std::vector<T> &v, cudaStream_t s) {
     if (!ensure(v.size() + 1)) return false;
@@ -72,17 +93,28 @@ struct DBuf {
   DBuf &operator=(const DBuf &) = delete;
 };
 
-// Grow-only pinned host buffer.
+// Pinned host buffers retired while an allocation stream was set: freeing
+// one (cudaFreeHost) waits for the whole device, so they are kept here until
+// free_retired_pinned() runs at a quiet point (the request server's shutdown).
+std::vector<void *> &retired_pinned();
+void retire_pinned(void *p);
+void free_retired_pinned();
+
+// Grow-only pinned host buffer; grows by at least half its size.
 struct PinnedBuf {
   char *p = nullptr;
   size_t cap = 0;
   bool ensure(size_t n) {
     if (n <= cap) return true;
-    if (p) cudaFreeHost(p);
+    if (p) {
+      if (alloc_stream()) retire_pinned(p);
+      else cudaFreeHost(p);
+    }
     p = nullptr;
+    const size_t want = std::max(n, cap + cap / 2);
     cap = 0;
-    if (cudaMallocHost((void **)&p, n) != cudaSuccess) return false;
-    cap = n;
+    if (cudaMallocHost((void **)&p, want) != cudaSuccess) return false;
+    cap = want;
     return true;
   }
   ~PinnedBuf() {
@@ -112,6 +144,15 @@ struct JobBuffers {
     return in.cap + 8 * (radius.cap + utab.cap + uL.cap + F.cap + cgeo.cap + usp.cap + ang.cap + out.cap + mat.cap) +
            4 * (gridEnd.cap + win.cap + status.cap + err.cap + live.cap + screenBlocks.cap) +
            8 * (head.cap + liveCount.cap);
+  }
+  // Releases the device buffers (ordered on stream s); they grow again on use.
+  void release(cudaStream_t s) {
+    in.release(s);
+    for (DBuf<double> *b : {&radius, &utab, &uL, &F, &cgeo, &usp, &ang, &out, &mat, &sout}) b->release(s);
+    for (DBuf<int> *b : {&gridEnd, &win, &status, &err, &live, &screenBlocks}) b->release(s);
+    head.release(s);
+    liveCount.release(s);
+    sphOff.release(s);
   }
   ~JobBuffers() {
     if (pinnedErr) cudaFreeHost(pinnedErr);

@@ -10,7 +10,13 @@
 //     and the AO matrix comes back, all on that stream, so jobs admitted while
 //     others are running overlap on the device;
 //   * completion is read from the slot's last event; the matrix is copied out
-//     of the pinned buffer and the slot is free again.
+//     of the pinned buffer and the slot is free again;
+//   * continuous batching at unit granularity: in the batched modes a served
+//     job's persistent CTAs each take at most kServeCtaUnits units and exit,
+//     so no job holds the SMs for its whole duration, and jobs below
+//     kSmallUnits units run on high-priority streams, whose pending CTAs the
+//     hardware places before those of the large jobs -- a small request that
+//     arrives while a large one runs starts within one CTA's units.
 // The basis-independent tables live in the engine and are shared by every
 // job; the level schedules are __constant__ data, so jobs in flight pin them
 // and a job whose large grid differs waits until the pins are released.
@@ -36,6 +42,9 @@ namespace ecpgb {
 
 namespace {
 
+constexpr int kServeCtaUnits = 8;            // units a served job's CTA takes before it exits
+constexpr long long kSmallUnits = 100000;    // (centre, pair) units below which a job is small
+
 double now_ms() {
   using namespace std::chrono;
   return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
@@ -58,7 +67,8 @@ struct Request {
 struct Slot {
   JobBuffers B;
   DevJob J{};
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;   // the stream of the current job
+  cudaStream_t hi = nullptr, lo = nullptr;  // high- and low-priority streams
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::shared_ptr<Request> req;
 };
@@ -107,11 +117,20 @@ struct Server {
     }
     r->tStart = now_ms();
     r->slot = k;
+    const long long units = (long long)r->P.nCentres * r->P.nPairs;
+    s.stream = units < kSmallUnits ? s.hi : s.lo;
+    // buffer growth ordered on the slot's stream: admitting a job never
+    // waits for the jobs running on the other slots
+    alloc_stream() = s.stream;
     bool ok = stage_job(r->P, T, s.B, s.J, mode, s.stream) == 0;
+    alloc_stream() = nullptr;
+    s.J.ctaUnits = kServeCtaUnits;
     ok = ok && cudaEventRecord(s.e0, s.stream) == cudaSuccess;
     ok = ok && run_pipeline(s.B, s.J, mode, nullptr, nullptr, nullptr, s.stream) == 0;
     const size_t mb = sizeof(double) * (size_t)r->P.dim * r->P.dim;
+    alloc_stream() = s.stream;  // a retired pinned buffer is freed later, not here
     ok = ok && s.B.pinnedOut.ensure(mb);
+    alloc_stream() = nullptr;
     ok = ok && cudaMemcpyAsync(s.B.pinnedOut.p, s.B.mat.p, mb, cudaMemcpyDeviceToHost, s.stream) == cudaSuccess;
     ok = ok && cudaMemcpyAsync(s.B.pinnedErr, s.B.err.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s.stream) ==
                    cudaSuccess;
@@ -184,11 +203,18 @@ struct Server {
           if (queue.empty()) break;
           r = queue.front();
         }
+        // the free slot that fits best: the smallest that holds the job
+        // without growing, else the largest
         int k = -1;
-        for (size_t i = 0; i < slots.size(); i++)
-          if (!slots[i]->req) { k = (int)i; break; }
+        for (size_t i = 0; i < slots.size(); i++) {
+          if (slots[i]->req) continue;
+          if (k < 0) { k = (int)i; continue; }
+          const size_t bi = slots[i]->B.device_bytes(), bk = slots[k]->B.device_bytes();
+          const bool fi = bi >= r->need, fk = bk >= r->need;
+          if ((fi && (!fk || bi < bk)) || (!fi && !fk && bi > bk)) k = (int)i;
+        }
         if (k < 0) break;
-        const size_t mine = slots[k]->B.device_bytes();
+        size_t mine = slots[k]->B.device_bytes();
         if (r->need > budget) {
           {
             std::lock_guard<std::mutex> lk(mu);
@@ -197,6 +223,18 @@ struct Server {
           r->err = "job needs more device memory than the server's budget";
           finish(*r, 3);
           continue;
+        }
+        // over the budget: release the buffers of idle slots, largest first
+        while (held() - mine + std::max(mine, r->need) > budget) {
+          int v = -1;
+          for (size_t i = 0; i < slots.size(); i++)
+            if ((int)i != k && !slots[i]->req && slots[i]->B.device_bytes() > 0 &&
+                (v < 0 || slots[i]->B.device_bytes() > slots[v]->B.device_bytes()))
+              v = (int)i;
+          if (v < 0) break;
+          slots[v]->B.release(slots[v]->stream);
+          std::lock_guard<std::mutex> lk(mu);
+          slotBytes[v] = 0;
         }
         if (held() - mine + std::max(mine, r->need) > budget) break;  // wait for memory
         int rc = start(k, r);
@@ -242,12 +280,16 @@ void *server_create(int mode, long long budget, int nSlots) {
   cudaGetDevice(&S->device);
   for (int k = 0; k < nSlots; k++) {
     auto s = std::make_unique<Slot>();
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (cudaStreamCreateWithPriority(&s->hi, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&s->lo, cudaStreamNonBlocking, least) != cudaSuccess ||
         cudaEventCreate(&s->e0) != cudaSuccess || cudaEventCreate(&s->e1) != cudaSuccess) {
       set_error("stream or event creation failed");
       delete S;
       return nullptr;
     }
+    s->stream = s->lo;
     S->slots.push_back(std::move(s));
   }
   S->slotBytes.assign(nSlots, 0);
@@ -350,12 +392,15 @@ void server_free(void *sv) {
   }
   if (S->worker.joinable()) S->worker.join();
   for (auto &s : S->slots) {
-    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (cudaStream_t st : {s->hi, s->lo})
+      if (st) cudaStreamSynchronize(st);
     if (s->e0) cudaEventDestroy(s->e0);
     if (s->e1) cudaEventDestroy(s->e1);
-    if (s->stream) cudaStreamDestroy(s->stream);
+    for (cudaStream_t st : {s->hi, s->lo})
+      if (st) cudaStreamDestroy(st);
   }
   delete S;
+  free_retired_pinned();
 }
 
 }  // namespace ecpgb
