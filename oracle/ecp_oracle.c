@@ -408,9 +408,14 @@ static int quad_ps93(const Sched *s, const double *w, int start, int end, double
     pts += cnt;
     n = s->lvN[k];
     p += (1 - j) * (I - q);
-    if (cnt > 0) err = 16 * fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q)) / (3 * n);
+    const double d = fabs((1 - j) * (q - 3 * p / 2) + j * (I - 2 * q));
+    if (cnt > 0) err = 16 * d / (3 * n);
     q = (1 - j) * q + j * I;
     if (cnt == 0) continue;
+    /* the GPU kernels test 16 d < tol 3 n (no divide); count the decisions
+       where that form and the reference's 16 d / (3 n) < tol disagree */
+    st->ps93_decisions++;
+    if ((err < tol) != (16 * d < tol * (3 * n))) st->ps93_divfree_flips++;
     /* d combines three running sums: its rounding error is below 3 nu,
        nu = kappa 2^-53 sabs, so err's is below 16 nu / n */
     if (decide(err < tol, err, tol, 16.0 * g_dec.kappa * 0x1p-53 * sabs / n)) {

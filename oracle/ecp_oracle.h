@@ -41,6 +41,9 @@ typedef struct {
   long long contraction_fma;  /* angular / polynomial contraction multiply-adds    */
   long long stale_reads;      /* fallback quadratures that read a point beyond the
                                  screened end (reference reuses stale buffers)     */
+  long long ps93_decisions;   /* small-grid error tests taken (levels with points) */
+  long long ps93_divfree_flips;/* of which 16 d < tol 3 n (the GPU's division-free
+                                 form) decides otherwise than 16 d / (3 n) < tol  */
 } OracleStats;
 
 /* Same semantics as getIntegrals: accumulates (+=) the upper triangle of the

@@ -30,7 +30,7 @@ class OracleStats(ct.Structure):
         "blocks", "ps93_calls", "ps93_points", "ps93_failed", "psm92_calls", "psm92_points",
         "psm92_failed", "t1_prim_pairs", "t1_fallback_pp", "t2_items", "t2_fallback_items",
         "t2_fallback_pp", "bessel_calls", "bessel_rows", "exp_calls", "table_points",
-        "contraction_fma", "stale_reads")]
+        "contraction_fma", "stale_reads", "ps93_decisions", "ps93_divfree_flips")]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}

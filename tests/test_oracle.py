@@ -152,3 +152,16 @@ def _spans(meta):
         n = ((m[2] + 1) * (m[2] + 2) // 2) * ((m[5] + 1) * (m[5] + 2) // 2)
         yield off, n
         off += n
+
+
+@pytest.mark.parametrize("name", ["cluster_subset_s0", "random_g_s101", "random_fL5_s200"])
+def test_division_free_ps93_test_takes_the_reference_decision(name):
+    """The GPU kernels test the PS93 error estimate as 16 d < tol 3 n instead of
+    16 d / (3 n) < tol.  The two forms can differ only where 16 d / (3 n) lies
+    within half an ulp of tol; on every small-grid decision of these fixtures'
+    systems (every level the reference tests) they take the same branch."""
+    s, _ = load_golden(name + ".npz")
+    rc, meta, data, st = O.oracle_blocks(s, with_stats=True)
+    assert rc == 0
+    assert st["ps93_decisions"] > 1000
+    assert st["ps93_divfree_flips"] == 0, st
