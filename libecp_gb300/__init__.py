@@ -389,9 +389,9 @@ class Job:
     def tune(self):
         """Runs the autotuner; returns (chosen, trials) as dicts."""
         chosen = LaunchConfig()
-        trials = (LaunchConfig * 16)()
+        trials = (LaunchConfig * 32)()
         n = ct.c_int(0)
-        rc = lib().ecpgb_job_tune(self._h, ct.byref(chosen), trials, 16, ct.byref(n))
+        rc = lib().ecpgb_job_tune(self._h, ct.byref(chosen), trials, 32, ct.byref(n))
         if rc:
             raise RuntimeError(f"ecpgb_job_tune failed ({rc}): {last_error()}")
         return chosen.as_dict(), [trials[i].as_dict() for i in range(n.value)]

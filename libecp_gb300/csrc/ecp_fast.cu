@@ -1532,7 +1532,11 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     }
     if (tid == 0) S.nextBase = 0;
     __syncthreads();
-    while (S.nextBase < nItems) {
+    // passes of up to kWalkCap failed items.  Thread 0 writes the pass's
+    // list, count and resume point before the barrier; every thread reads
+    // the count after it, and thread 0 writes again only after the pass's
+    // last barrier, so no thread can see the next pass's values early.
+    for (;;) {
       if (tid == 0) {
         int nf = 0, q = S.nextBase;
         unsigned mask = 0;
@@ -1556,6 +1560,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       }
       __syncthreads();
       const int nf = S.nThis;
+      if (nf == 0) break;  // no failed item left
       double *W = ph + warp * Lm.w2Stride;
       for (int q = tid & 31; q < nf; q += 32) W[Lm.w2Part + q] = 0.0;
       __syncwarp();
