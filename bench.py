@@ -225,6 +225,7 @@ def ours(args, rank, world):
     if mode == eg.ECPGB_FAST:
         # the autotuner picks the launch configuration (outside the timed region)
         chosen, trials = job.tune()
+        chosen["class_config"] = job.class_config()
         tuned = {"chosen": chosen, "trials": trials}
     job.run(args.warmup, flush_l2=True)
     n_units, emitted = job.units()
@@ -289,6 +290,7 @@ def ours(args, rank, world):
         from libecp_gb300.precision import oracle_class_errors
         mj = eg.Job(system, mode=eg.ECPGB_MIXED)
         mchosen, _ = mj.tune()
+        mchosen["class_config"] = mj.class_config()
         mj.run(args.warmup, flush_l2=True)
         mms, mmu = mj.run(args.steps, flush_l2=True)
         mj.close()

@@ -149,10 +149,13 @@ void ecpgb_job_free(ecpgb_job *j);
  * the primitive pairs per warp and the CTAs per SM; balance: 1 = a unit with
  * few primitive pairs gets narrower type-1 groups so that all its warps
  * work; screen: 1 = with the queue launch, a screening stage first compacts
- * the queue to the units that compute blocks.  msUnit: the unit kernel's
- * time when the autotuner measured it, else 0. */
+ * the queue to the units that compute blocks.  perClass: 1 = the autotuner
+ * chose the type-1 cap and balance per (la, lb) class (see
+ * ecpgb_job_class_config; gcap is then the cap the shared memory is sized
+ * for); configurations set with ecpgb_job_config have none.  msUnit: the
+ * unit kernel's time when the autotuner measured it, else 0. */
 typedef struct {
-  int queue, sorted, gcap, balance, screen;
+  int queue, sorted, gcap, balance, screen, perClass;
   float msUnit;
 } ecpgb_launch_config;
 
@@ -167,6 +170,11 @@ typedef struct {
  * 0 ok, 1 error, 3 the job is not a batched-path job. */
 int ecpgb_job_tune(ecpgb_job *j, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials,
                    int *nTrials);
+/* The per-class type-1 settings of the job's configuration: for class
+ * c = la * (max basis l + 1) + lb, c < n (at most 25), gcap[c] and
+ * balance[c], or 0 and -1 where the class uses the job-wide gcap and balance.
+ * 0 ok, 1 error. */
+int ecpgb_job_class_config(ecpgb_job *j, int n, int *gcap, int *balance);
 /* Sets (cfg != NULL) and/or reads (out != NULL) the job's configuration. */
 int ecpgb_job_config(ecpgb_job *j, const ecpgb_launch_config *cfg, ecpgb_launch_config *out);
 /* 1: ecpgb_job_run replays the pipeline as one captured CUDA graph (the

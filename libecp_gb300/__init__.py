@@ -50,7 +50,7 @@ class EcpgbInfo(ct.Structure):
 class LaunchConfig(ct.Structure):
     """ecpgb_launch_config: batched-path launch configuration."""
     _fields_ = [("queue", ct.c_int), ("sorted", ct.c_int), ("gcap", ct.c_int), ("balance", ct.c_int),
-                ("screen", ct.c_int), ("msUnit", ct.c_float)]
+                ("screen", ct.c_int), ("perClass", ct.c_int), ("msUnit", ct.c_float)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -120,6 +120,8 @@ def lib() -> ct.CDLL:
     L.ecpgb_job_tune.restype = ct.c_int
     L.ecpgb_job_config.argtypes = [ct.c_void_p, ct.POINTER(LaunchConfig), ct.POINTER(LaunchConfig)]
     L.ecpgb_job_config.restype = ct.c_int
+    L.ecpgb_job_class_config.argtypes = [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int)]
+    L.ecpgb_job_class_config.restype = ct.c_int
     L.ecpgb_job_use_graph.argtypes = [ct.c_void_p, ct.c_int]
     L.ecpgb_job_use_graph.restype = ct.c_int
     L.ecpgb_job_blocks.argtypes = [ct.c_void_p, _D, _I]
@@ -407,10 +409,25 @@ class Job:
                            cur.sorted if sorted is None else int(sorted),
                            cur.gcap if gcap is None else int(gcap),
                            cur.balance if balance is None else int(balance),
-                           cur.screen if screen is None else int(screen), 0.0)
+                           cur.screen if screen is None else int(screen), 0, 0.0)
         if lib().ecpgb_job_config(self._h, ct.byref(new), ct.byref(cur)):
             raise RuntimeError(last_error())
         return cur.as_dict()
+
+    def class_config(self) -> dict:
+        """Per-(la, lb)-class type-1 settings of the configuration:
+        {"la,lb": {"gcap": g, "balance": b}} for the classes the autotuner set."""
+        n = 25
+        g = (ct.c_int * n)()
+        b = (ct.c_int * n)()
+        if lib().ecpgb_job_class_config(self._h, n, g, b):
+            raise RuntimeError(last_error())
+        lb1 = self.system.max_l_basis() + 1 + getattr(self.system, "derivative", 0)
+        out = {}
+        for i in range(min(n, lb1 * lb1)):
+            if g[i]:
+                out[f"{i // lb1},{i % lb1}"] = {"gcap": int(g[i]), "balance": int(b[i])}
+        return out
 
     def use_graph(self, on: bool = True) -> None:
         if lib().ecpgb_job_use_graph(self._h, int(on)):

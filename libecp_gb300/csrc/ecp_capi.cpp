@@ -264,6 +264,10 @@ int ecpgb_job_config(ecpgb_job *j, const ecpgb_launch_config *cfg, ecpgb_launch_
   return j ? ecpgb::job_config(j->impl, cfg, out) : 1;
 }
 
+int ecpgb_job_class_config(ecpgb_job *j, int n, int *gcap, int *balance) {
+  return j ? ecpgb::job_class_config(j->impl, n, gcap, balance) : 1;
+}
+
 int ecpgb_job_use_graph(ecpgb_job *j, int on) { return j ? ecpgb::job_use_graph(j->impl, on) : 1; }
 
 int ecpgb_job_blocks(ecpgb_job *j, double *values, int *status) {

@@ -42,6 +42,10 @@ enum : int {
   kUnitWarnType2 = 3,   // written; the same for a type-2 quadrature only
 };
 
+// Per-class launch settings (ecp_fast.cu): classes (la, lb) with la, lb <= 4.
+constexpr int kMaxClasses = 25;
+constexpr int kClassSet = 1 << 20;
+
 struct DevJob {
   // sizes
   int nAtoms, nShells, nPrims, nCentres, nPairs, dim;
@@ -105,6 +109,10 @@ struct DevJob {
   int mixed;                     // 1: the fallbacks' tables and sums in double-single (ecp_ff.h)
   int balance;                   // 1: type-1 groups narrowed so that every warp gets pairs
   int ctaUnits;                  // >0: a persistent CTA takes at most this many units, then exits
+  // per-(la, lb)-class type-1 settings (index la * (maxLBS + 1) + lb):
+  // 0 = the job's gcap and balance, else kClassSet | gcap | balance << 12
+  int classCfg[kMaxClasses];
+  unsigned long long *classCycles;  // non-null: clock cycles of each class's units (autotuner)
   // screening stage (batched path): the queue of units that compute blocks
   int *live;                     // live units in queue order (null: no screening stage)
   unsigned long long *liveCount; // their number
@@ -119,6 +127,10 @@ struct FastConfig {
   int mixed = 0;   // set from the job's mode (ECPGB_MIXED), not tuned
   int balance = 1; // narrower type-1 groups when a unit has few primitive pairs
   int screen = 1;  // with the queue launch: a screening stage compacts the queue to live units
+  // per-(la, lb)-class type-1 cap and balance (DevJob::classCfg); the launch's
+  // shared memory is sized by gcap, so a class's cap is at most gcap
+  int cls[kMaxClasses] = {};
+  unsigned long long *classCycles = nullptr;  // autotuner: per-class cycle counts
 };
 
 // Shared-memory layout of the unit kernel (offsets in doubles).

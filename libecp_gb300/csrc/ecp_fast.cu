@@ -1283,6 +1283,14 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
   }
   const FastSmem Lm = fast_layout(J.maxLBS, J.maxLECP, J.gcap, J.maxNP);
   const int A = J.shAtom[sa], B = J.shAtom[sb], la = J.shL[sa] + sh.a, lb = J.shL[sb] + sh.b, lab = la + lb;
+  // the class's type-1 settings (the autotuner may set them per (la, lb))
+  const int cls = la * (J.maxLBS + 1) + lb;
+  int gcapU = J.gcap, balU = J.balance;
+  if (J.classCfg[cls] & kClassSet) {
+    gcapU = J.classCfg[cls] & 0xfff;
+    balU = (J.classCfg[cls] >> 12) & 1;
+  }
+  const long long tc0 = J.classCycles ? clock64() : 0;
   const int lpa = sh.lpa, lpb = sh.lpb, pa0 = sh.a > 0 ? sh.a : 0, pb0 = sh.b > 0 ? sh.b : 0;
   const int nA = 2 * J.maxLBS + 1, LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE;
   const int Lc = J.ctrL[c], nca = NCUM(la), ncb = NCUM(lb), O = kSmallOrder;
@@ -1389,9 +1397,9 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     int Gk[3], nG[3], nGroups = 0;
     for (int kd = 0; kd < 3; kd++) {
       const int n = S.t1Count[kd];
-      int G = t1_group(lab, J.gcap);
+      int G = t1_group(lab, gcapU);
       // balance: with few primitive pairs, narrower groups keep all warps busy
-      if (J.balance) {
+      if (balU) {
         const int Gb = (n + kWarps - 1) / kWarps;
         if (Gb < G) G = Gb > 0 ? Gb : 1;
       }
@@ -1615,6 +1623,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     int st = (S.warn & 1) ? kUnitWarnType1 : (S.warn & 2) ? kUnitWarnType2 : kUnitDone;
     J.status[u] = st;
     if (st != kUnitDone) atomicMin(&J.errWord[0], (int)u);
+    if (J.classCycles) atomicAdd(&J.classCycles[cls], (unsigned long long)(clock64() - tc0));
   }
 }
 
@@ -1817,6 +1826,8 @@ int launch_fast_pipeline(const DevJob &J, cudaStream_t st, size_t smemBytes, con
   Jc.gcap = cfg.gcap;
   Jc.mixed = cfg.mixed;
   Jc.balance = cfg.balance;
+  for (int i = 0; i < kMaxClasses; i++) Jc.classCfg[i] = cfg.cls[i];
+  Jc.classCycles = cfg.classCycles;
   if (!cfg.sorted) Jc.order = nullptr;
   else if (cfg.sorted == 2 && J.orderClass) Jc.order = J.orderClass;
   const bool screen = cfg.queue && cfg.screen && J.queueHead && J.live && J.liveCount && J.screenBlocks;

@@ -257,6 +257,7 @@ struct Engine {
   const DevTables *schedOwner = nullptr;
   JobBuffers shared;
   DBuf<char> flush;
+  DBuf<unsigned long long> classCycles;  // autotuner: per-class cycle counts
   DBuf<double> dens, gradBuf;  // density matrix and gradient of run_gradient
   bool init = false;
 
@@ -1035,7 +1036,21 @@ int job_run(void *vj, int nRuns, int flushL2, float *msRun, float *msUnit) {
 }
 
 static ecpgb_launch_config to_c(const FastConfig &c, float ms) {
-  return {c.queue, c.sorted, c.gcap, c.balance, c.screen, ms};
+  int per = 0;
+  for (int i = 0; i < kMaxClasses; i++) per |= (c.cls[i] & kClassSet) ? 1 : 0;
+  return {c.queue, c.sorted, c.gcap, c.balance, c.screen, per, ms};
+}
+
+int job_class_config(void *vj, int n, int *gcap, int *balance) {
+  Engine &E = engine();
+  std::lock_guard<std::mutex> lk(E.mu);
+  auto *R = (ResidentJob *)vj;
+  for (int i = 0; i < n && i < kMaxClasses; i++) {
+    const int v = R->cfg.cls[i];
+    if (gcap) gcap[i] = (v & kClassSet) ? (v & 0xfff) : 0;
+    if (balance) balance[i] = (v & kClassSet) ? ((v >> 12) & 1) : -1;
+  }
+  return 0;
 }
 
 int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials, int *nTrials) {
@@ -1094,6 +1109,69 @@ int job_tune(void *vj, ecpgb_launch_config *chosen, ecpgb_launch_config *trials,
     if (trials && n < maxTrials) trials[n] = to_c(c, ms);
     n++;
     if (ms < best) { best = ms; bestCfg = c; }
+  }
+  // per-class refinement on the best persistent configuration: each
+  // (la, lb) class takes the type-1 cap (at most the launch's) and balance
+  // under which its own units took the fewest cycles, measured with every
+  // class on one setting at a time; the combination is kept if the whole job
+  // runs faster with it
+  if (bestCfg.queue == 1 && E.classCycles.ensure(kMaxClasses)) {
+    struct Opt { int gcap, balance; };
+    std::vector<Opt> opts;
+    for (int gcap : {45, 33})
+      for (int bal : {0, 1})
+        if (gcap <= bestCfg.gcap) opts.push_back({gcap, bal});
+    std::vector<std::vector<unsigned long long>> cyc;
+    bool ok = true;
+    for (const Opt &o : opts) {
+      FastConfig c = bestCfg;
+      for (int i = 0; i < kMaxClasses; i++) c.cls[i] = kClassSet | o.gcap | o.balance << 12;
+      c.classCycles = E.classCycles.p;
+      cudaMemsetAsync(E.flush.p, 0x5a, flushBytes, E.stream);
+      cudaMemsetAsync(E.classCycles.p, 0, sizeof(unsigned long long) * kMaxClasses, E.stream);
+      std::vector<unsigned long long> h(kMaxClasses, 0);
+      if (run_pipeline(R->B, R->J, R->mode, nullptr, nullptr, &c, E.stream) ||
+          cudaMemcpyAsync(h.data(), E.classCycles.p, sizeof(unsigned long long) * kMaxClasses,
+                          cudaMemcpyDeviceToHost, E.stream) != cudaSuccess ||
+          cudaStreamSynchronize(E.stream) != cudaSuccess) {
+        ok = false;
+        break;
+      }
+      cyc.push_back(h);
+    }
+    if (ok && !opts.empty()) {
+      FastConfig comb = bestCfg;
+      for (int i = 0; i < kMaxClasses; i++) {
+        size_t bo = 0;
+        for (size_t o = 1; o < opts.size(); o++)
+          if (cyc[o][i] < cyc[bo][i]) bo = o;
+        comb.cls[i] = kClassSet | opts[bo].gcap | opts[bo].balance << 12;
+      }
+      float tot = 0;
+      for (int r = 0; r < 3 && ok; r++) {
+        cudaMemsetAsync(E.flush.p, r & 0xff, flushBytes, E.stream);
+        if (run_pipeline(R->B, R->J, R->mode, u0, u1, &comb, E.stream) ||
+            cudaStreamSynchronize(E.stream) != cudaSuccess) {
+          ok = false;
+          break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, u0, u1);
+        if (r) tot += ms;
+      }
+      if (ok) {
+        const float ms = tot / 2;
+        if (trials && n < maxTrials) trials[n] = to_c(comb, ms);
+        n++;
+        if (ms < best) { best = ms; bestCfg = comb; }
+      }
+    }
+    if (!ok) {
+      cudaEventDestroy(u0);
+      cudaEventDestroy(u1);
+      set_error("per-class tuning failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return 1;
+    }
   }
   cudaEventDestroy(u0);
   cudaEventDestroy(u1);

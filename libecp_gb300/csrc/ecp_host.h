@@ -175,6 +175,7 @@ int job_launches(const void *j);
 void job_free(void *j);
 int job_tune(void *j, ecpgb_launch_config *chosen, ecpgb_launch_config *trials, int maxTrials, int *nTrials);
 int job_config(void *j, const ecpgb_launch_config *cfg, ecpgb_launch_config *out);
+int job_class_config(void *j, int n, int *gcap, int *balance);
 int job_use_graph(void *j, int on);
 int job_blocks(void *j, double *values, int *status);
 int measure_peaks(double *out);

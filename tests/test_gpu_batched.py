@@ -106,3 +106,23 @@ def test_screening_stage_marks_the_same_units(eg, system):
     _, s = _run(eg, j, queue=1, screen=1)
     assert np.array_equal(s, ref_s) and (s == 1).any() and (s != 1).any()
     j.close()
+
+
+def test_per_class_settings_stay_within_parity(eg, system):
+    """The autotuner's per-(la, lb) refinement: every class it sets has a cap
+    within the launch's and a balance of 0 or 1, and the tuned job matches the
+    FP64 path within the bar."""
+    jp = eg.Job(system, mode=eg.ECPGB_FP64)
+    ref_v, ref_s = _run(eg, jp)
+    jp.close()
+    j = eg.Job(system, mode=eg.ECPGB_FAST)
+    chosen, trials = j.tune()
+    cls = j.class_config()
+    assert bool(cls) == bool(chosen["perClass"])
+    for key, c in cls.items():
+        assert 1 <= c["gcap"] <= chosen["gcap"] and c["balance"] in (0, 1), (key, c)
+    assert any(t["perClass"] for t in trials) or chosen["queue"] != 1
+    v, s = _run(eg, j)
+    assert np.array_equal(s, ref_s)
+    assert np.abs(v - ref_v).max() <= TOL_ABS
+    j.close()
