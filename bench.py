@@ -322,9 +322,10 @@ def ours(args, rank, world):
         # unit (ncu: 2 DFMA + DMUL + DADD thread instructions of one launch on
         # the cluster's first 8 centres, divided by its emitted units), FP64
         # pipe utilisation and DRAM bytes, from profiles/roofline_inputs.txt
+        # (measured on the cluster: other workloads have no executed-work figure)
         entry = {}
         prof = os.path.join(ROOT, "profiles", "roofline_inputs.txt")
-        if os.path.exists(prof):
+        if os.path.exists(prof) and args.workload == "cluster":
             with open(prof) as f:
                 inputs = json.load(f)
             key = {"k_unit": "k_unit", "k_unit_queue": "k_unit_queue", "k_unit_fast": "k_unit_queue"}[kernel]

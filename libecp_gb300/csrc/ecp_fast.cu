@@ -382,6 +382,7 @@ static __device__ bool ps93_walk_fast(const double *w, int start, int end, doubl
       return true;
     }
   }
+  res = 16 * q / (3 * c93_lvN[c93_nLevels - 1]);  // the last estimate (mixed path: its size)
   return false;
 }
 
@@ -622,7 +623,16 @@ struct FastShared {
   unsigned passMask;            // channels read by this pass's failed quadratures
   int passL1, passL2, passL3;   // highest Ka, Kb and r^l rows they read
   int warn;
+  unsigned long long estBits;   // mixed path: largest |estimate| of a failed small-grid item (bits)
 };
+
+// Mixed path: the largest quadrature value for which double-single level
+// sums still decide the large-grid convergence test as FP64 does.  The
+// test 16 e^2 <= 3 N |I - q| tol needs the noise of e and I - q, about
+// 2^-47 of the integral in double-single, well below 3 N tol / 16; at the
+// coarsest levels (N = 256) that noise reaches it for integrals near
+// 2^47 tol 48, so quadratures above 1/64 of that take FP64 tables.
+__device__ inline double ff_limit(double tol) { return 0x1p47 * tol * 0.75; }
 
 // --------------------------------------------------------------- type 1
 
@@ -892,6 +902,16 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
   for (int gg = 0; gg < G; gg++) {
     const bool fail = failed && g == gg;
     if (!__ballot_sync(0xffffffffu, fail)) continue;
+    // mixed path: the pair's tables in double-single only where the sums of
+    // its failed quadratures can take the reference's decisions (ff_limit,
+    // judged on their last small-grid estimates); larger integrals in FP64
+    bool ffp = false;
+    if constexpr (kMixed) {
+      const double est = fail ? fabs(16 * q / (3 * c93_lvN[c93_nLevels - 1])) : 0.0;
+      const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(est) >> 32);
+      const unsigned lim = (unsigned)((unsigned long long)__double_as_longlong(ff_limit(J.tol)) >> 32);
+      ffp = __reduce_max_sync(0xffffffffu, hi) < lim;
+    }
     const int kk = perm[p0 + gg];
     const double za = pzA[kk / Nb], ca = zeta_times(pcA[kk / Nb], za, pa0), zb = pzB[kk % Nb],
                  cb = zeta_times(pcB[kk % Nb], zb, pb0);
@@ -945,7 +965,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
         if (n < nb && !(upper && n > end)) {
           double r = i1 * J.xLarge[n] + i2, ex = (z * r + s) * r + zd2;
           if (ex >= J.lnAcc1) {
-            if constexpr (kMixed) {
+            if (ffp) {
               ff *Kf = (ff *)K, *WRf = (ff *)WR;
               const ff rf = ff_from_double(r);
               ff v = ff_mul(ff_mul(J.wLf[n], i1f),
@@ -984,7 +1004,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
               WR[l] = ok ? v * pw : 0.0;
               K[l] = ok ? bessel_row(J, lr, s * xr) : 0.0;
             }
-            if constexpr (kMixed)  // the rows as ff, in place (entry l holds row l either way)
+            if (ffp)  // the rows as ff, in place (entry l holds row l either way)
               for (int l = 0; l <= lab; l++) {
                 ((ff *)WR)[l] = ff_from_double(WR[l]);
                 ((ff *)K)[l] = ff_from_double(K[l]);
@@ -999,7 +1019,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       __syncwarp();
       if (!done2) {
         auto vis = [&](int t) { return c92_slot[t] <= end; };
-        if constexpr (kMixed) {
+        if (ffp) {
           auto val = [&](int t) {
             const ff *e = (const ff *)(tab + (t - s0) * TSf);
             return ff_mul(e[lq + l1], e[l2]);
@@ -1334,7 +1354,11 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
                                    },
                                    res);
     if (ok) T[tidx(l, l1, l2, l3)] = res;
-    else { atomicOr(&S.failMask[q >> 5], 1u << (q & 31)); atomicAdd(&S.nFail, 1); }
+    else {
+      atomicOr(&S.failMask[q >> 5], 1u << (q & 31));
+      atomicAdd(&S.nFail, 1);
+      if (kMixed) atomicMax(&S.estBits, (unsigned long long)__double_as_longlong(fabs(res)));
+    }
   };
   for (int e = tid; e < LE * LBE * LBE * nA; e += NT) T[e] = 0.0;
   for (int e = tid; e < 64; e += NT) S.failMask[e] = 0;
@@ -1342,6 +1366,7 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
     S.warn = 0;
     S.nFail = 0;
     S.t2Next = 0;
+    S.estBits = 0ull;
   }
   __syncthreads();
 
@@ -1572,9 +1597,17 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       double *W = ph + warp * Lm.w2Stride;
       for (int q = tid & 31; q < nf; q += 32) W[Lm.w2Part + q] = 0.0;
       __syncwarp();
-      for (int k = warp; k < NP; k += kWarps)
-        t2_pair<kMixed>(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0, ph + Lm.ppMap,
-                (const int *)(ph + Lm.ppWin), warn2);
+      // mixed path: double-single tables only where their sums can take the
+      // reference's decisions (ff_limit); larger integrals in FP64
+      const bool ff2 = kMixed && __longlong_as_double((long long)S.estBits) < ff_limit(J.tol);
+      for (int k = warp; k < NP; k += kWarps) {
+        if (ff2)
+          t2_pair<kMixed>(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0,
+                          ph + Lm.ppMap, (const int *)(ph + Lm.ppWin), warn2);
+        else
+          t2_pair<false>(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0,
+                         ph + Lm.ppMap, (const int *)(ph + Lm.ppWin), warn2);
+      }
       __syncthreads();
       for (int q = tid; q < nf; q += NT) {
         double v = 0.0;

@@ -83,6 +83,14 @@ def bar_scaled(ref_block, scale) -> float:
     return TOL_ABS + SCALE_UNITS * 2.0 ** -53 * float(scale)
 
 
+# Bar of the mixed-precision path: double-single carries about 2^-48 of a
+# block's scale where FP64 carries 2^-53, so 2^-44 of the scale replaces the
+# FP64 bar's 128 units of 2^-53 (on the 50-centre cluster, where the scales
+# stay below 1e6, the two differ by less than 1e-10).
+def bar_mixed(ref_block, scale) -> float:
+    return TOL_ABS + 2.0 ** -44 * float(scale)
+
+
 # Rounding-noise bound (in units of 2^-53 times the sum of |w f| of a
 # quadrature) within which the oracle marks a convergence decision as
 # ambiguous and offers the inverted branch (oracle_blocks_alt).  The GPU

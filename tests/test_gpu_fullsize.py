@@ -4,7 +4,7 @@ ECP centres) and the high-accuracy sweep (447 shells, 99,681 pairs, l <= 4, L
 <= 5 with 6 terms, exponents 0.01-500).
 
 The whole workload runs on the GPU in both FP64 paths (plain drop-in and
-batched); a seeded sample of sub-systems -- one ECP centre and three basis
+batched) and in the mixed-precision path; a seeded sample of sub-systems -- one ECP centre and three basis
 atoms, plus the atoms that keep the full system's table sizes -- is computed
 by the oracle, and every block of the sample is compared with the GPU's block
 of the same (centre, shell pair) from the full run.
@@ -12,7 +12,8 @@ of the same (centre, shell pair) from the full run.
 Bar: helpers.bar_scaled (1e-10, plus 128 * 2^-53 of the block's scale, its
 largest element evaluated over absolute values: the rounding any correct FP64
 evaluation carries where the shift onto A and B cancels terms ~1e7 times
-larger than the result).
+larger than the result); helpers.bar_mixed (2^-44 of the scale) for the
+mixed-precision path.
 Decisions the reference takes within rounding noise (a quadrature's error
 test within helpers.KAPPA_FP64 * 2^-53 * sum |w f| of its tolerance) can go
 either way in another correct FP64 evaluation; a block also passes when it
@@ -25,7 +26,7 @@ import pytest
 
 from libecp_gb300 import workloads as W
 from oracle import oracle as O
-from tests.helpers import KAPPA_FP64, bar_scaled, size_preserving_subset
+from tests.helpers import KAPPA_FP64, bar_mixed, bar_scaled, size_preserving_subset
 
 pytestmark = pytest.mark.gpu
 
@@ -67,7 +68,7 @@ def test_full_size_sampled_against_oracle(eg, name):
         s = W.mixed_batch(0) if name == "mixed" else W.large_sweep(0)
         units = eg.unit_table(s)
         index = {(u[6], u[0], u[1], u[3], u[4]): i for i, u in enumerate(units)}
-        gpu = {mode: eg.raw_blocks(s, mode) for mode in (eg.ECPGB_FP64, eg.ECPGB_FAST)}
+        gpu = {mode: eg.raw_blocks(s, mode) for mode in (eg.ECPGB_FP64, eg.ECPGB_FAST, eg.ECPGB_MIXED)}
         results = oracle.get()
     report = []
     for mode, (v, offs, st, info) in gpu.items():
@@ -82,7 +83,8 @@ def test_full_size_sampled_against_oracle(eg, name):
                 assert st[u] != eg.UNIT_SKIPPED
                 n = ((la + 1) * (la + 2) // 2) * ((lb + 1) * (lb + 2) // 2)
                 got.append(v[offs[u] + (typ - 1) * n: offs[u] + typ * n])
-            res = O.match_blocks(meta, np.concatenate(got), meta, data, am, ad, bar_scaled, scale)
+            bar = bar_mixed if mode == eg.ECPGB_MIXED else bar_scaled
+            res = O.match_blocks(meta, np.concatenate(got), meta, data, am, ad, bar, scale)
             failures += [(f[0], f"{f[1]:.3e}", f"{f[2]:.3e}", int(st[index[(f[0][6], f[0][0], f[0][1], f[0][3],
                                                                               f[0][4])]]))
                          for f in res["failures"]]

@@ -15,17 +15,13 @@ import pytest
 
 from libecp_gb300 import workloads as W
 from oracle import oracle as O
-from tests.helpers import TOL_ABS, golden_files, load_golden
+from tests.helpers import TOL_ABS, bar_mixed, golden_files, load_golden
 from tests.test_gpu_parity import CASES
-
-
-def mixed_bar(ref_block, scale):
-    return TOL_ABS + 2.0 ** -44 * float(scale)
 
 
 def assert_mixed_match(s, meta, data):
     rc, mo, do, am, ad, sc = O.oracle_blocks_alt(s, 16.0)
-    res = O.match_blocks(meta, data, mo, do, am, ad, mixed_bar, sc)
+    res = O.match_blocks(meta, data, mo, do, am, ad, bar_mixed, sc)
     assert not res["failures"], res["failures"][:5]
 
 
