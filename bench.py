@@ -1,21 +1,25 @@
 """Benchmark: ECP shell-pair integrals/s on the batched 50-centre cluster.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--mode batched|fp64] [--serve-rate R] [--serve-seconds S]
+                    [--mode batched|fp64] [--workload cluster|mixed_batch|sweep|...]
+                    [--serve-rate R] [--serve-seconds S] [--serve-mixed-seconds S]
+                    [--mixed-report 0|1] [--compare-plain 0|1]
 
-Workload (per rank): the batched cluster -- 50 ECP centres (L up to 4, 2-6
-terms per channel), 63 contracted shells (l = 0..3 with weights
+Workload (per rank, default): the batched cluster -- 50 ECP centres (L up to
+4, 2-6 terms per channel), 63 contracted shells (l = 0..3 with weights
 .4/.3/.2/.1, contraction 1..8) giving 2016 shell pairs, i.e. 100,800
 (shell pair, centre) units of which the screening keeps ~91k.  A step is one
 pass of the whole getIntegrals path over that job: shell radii, centre
 potentials, angular tables, F tables, every unit's type-1 and type-2 block,
 and the AO-matrix scatter.  The unit of the metric is one emitted unit (a
-type-1 + type-2 block pair handed to the reference's callback).
+type-1 + type-2 block pair handed to the reference's callback).  The other
+workloads (--workload) are the 20,000-pair mixed batch and the 100,000-pair
+high-accuracy sweep.
 
 Path: the batched FP64 engine (ECPGB_FAST) by default -- the autotuner picks
-its launch configuration first, then the job replays as a captured CUDA
-graph; the plain FP64 drop-in kernels (ECPGB_FP64) run two steps on the same
-job for the batched / plain ratio.
+its launch configuration first (including per-(la, lb)-class settings), then
+the job replays as a captured CUDA graph; the plain FP64 drop-in kernels
+(ECPGB_FP64) run two steps on the same job for the batched / plain ratio.
 
 value   : device-resident job (inputs in HBM before the timed region); per step
           CUDA events on the engine's stream; L2 flushed (256 MiB write) between
@@ -23,12 +27,22 @@ value   : device-resident job (inputs in HBM before the timed region); per step
 e2e     : ecpgb_getIntegrals (the getIntegrals call with the path chosen) with
           host buffers: one packed H2D copy of the inputs and a D2H copy of the
           matrix per step.
-roofline: the per-unit kernel against the measured FP64 FMA pipe (the path is
-          FP64-arithmetic bound; HBM traffic is tiny); algorithmic FLOPs are
-          counted on the oracle's run of the reference control flow over the
-          CPU-baseline sample and scaled per unit.
-serving : a Poisson stream of molecules through the request server (continuous
-          batching), latency percentiles from the server's own clock.
+roofline: the unit kernel against the FP64 FMA pipe measured live (the path is
+          FP64-latency bound; DRAM traffic is a few hundred bytes per unit):
+          achieved = FP64 operations the kernel executed per emitted unit (ncu
+          counts on the cluster's first 8 centres, profiles/roofline_inputs.txt;
+          cluster workload only) x emitted units / the unit kernel's CUDA-event
+          time; alg_* = the reference's algorithmic FLOPs counted by the oracle
+          on its control flow over the CPU-baseline sample.
+cpu_baseline: the oracle restatement (or the reference build where one exists
+          on the machine) on a bounded sample of the workload, on all host cores
+          the process may use and on one core.
+mixed_precision: the mixed-precision engine on the same job: speed, its error
+          against the plain FP64 path over every unit, and per L class against
+          the oracle on the job's first two ECP centres.
+serving : Poisson streams of molecules through the request server (continuous
+          batching) near one GPU's capacity, FP64 and mixed precision, latency
+          percentiles from the server's own clock.
 Multi-GPU: weak scaling, one independent cluster per rank (seed = rank), no
           collective on the data path; max over ranks of the timed span.
 """
