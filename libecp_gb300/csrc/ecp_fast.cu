@@ -800,14 +800,18 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
         if (run >> (gg * nq) & qm) live |= 1u << gg;
     }
     const int nLive = __popc(live);
-    // the i-th live pair of the group
-    auto live_pair = [&](int i) {
-      unsigned m = live;
-      for (; i > 0; i--) m &= m - 1u;
-      return __ffs(m) - 1;
-    };
+    // the live pairs' indices, 4 bits each (G <= 8), and entry e's (slot,
+    // live pair) = (e / nLive, e % nLive) with the quotient by a
+    // multiply-shift: ceil(2^16 / d) is exact for d <= 8 and e < 8192
+    // (e < 33 * 8 here) -- no integer divide in the loops
+    unsigned packed = 0;
+    for (unsigned m = live, j = 0; m; m &= m - 1u, j++) packed |= (unsigned)(__ffs(m) - 1) << (4 * j);
+    const unsigned dmag = nLive > 0 ? (65536u + (unsigned)nLive - 1u) / (unsigned)nLive : 0u;
+    auto slot_of = [&](int e) { return (int)(((unsigned)e * dmag) >> 16); };
+    auto live_pair = [&](int e, int i) { return (int)((packed >> (4 * (e - i * nLive))) & 15u); };
     for (int e = lane; e < nIn * nLive; e += 32) {
-      const int gg = live_pair(e % nLive), t = __ldg(J.byN93 + s0 + lo + e / nLive), n = __ldg(J.s93 + t);
+      const int i = slot_of(e);
+      const int gg = live_pair(e, i), t = __ldg(J.byN93 + s0 + lo + i), n = __ldg(J.s93 + t);
       double *ent = tab + ((t - s0) * G + gg) * TSs;
       const double s = sc[gg * 6];
       double *WR = ent + lq;
@@ -835,8 +839,8 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       }
     }
     for (int e = lane; e < (ns - nIn) * nLive; e += 32) {
-      const int i = e / nLive, t = __ldg(J.byN93 + s0 + (i < lo ? i : i + nIn));
-      double *ent = tab + ((t - s0) * G + live_pair(e % nLive)) * TSs;
+      const int i = slot_of(e), t = __ldg(J.byN93 + s0 + (i < lo ? i : i + nIn));
+      double *ent = tab + ((t - s0) * G + live_pair(e, i)) * TSs;
       for (int l = 0; l <= 2 * lq; l++) ent[l] = 0.0;
     }
     __syncwarp();
@@ -1117,7 +1121,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       if (owner >= 0 && S.ppBreak[owner] == n) owner = -1;
     }
     if (owner < 0) return;
-    const double zaj = pzA[owner / Nb], zbj = pzB[owner % Nb];
+    const double zaj = owner == k ? za : pzA[owner / Nb], zbj = owner == k ? zb : pzB[owner % Nb];
     r = map[2 * owner] * J.xLarge[n] + map[2 * owner + 1];
     const double d1 = dAC - r, d2 = dBC - r;
     ex = -zaj * d1 * d1 - zbj * d2 * d2;
@@ -1175,7 +1179,8 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       int owner;
       double r, ex;
       locate(t, owner, r, ex);
-      const double zaj = pzA[owner / Nb], zbj = pzB[owner % Nb];
+      // the pair's own exponents (no integer divide) unless a stale slot
+      const double zaj = owner == k ? za : pzA[owner / Nb], zbj = owner == k ? zb : pzB[owner % Nb];
       double *e = tab + lane * TS;
       if constexpr (kMixed) {
         // the same rows in double-single
