@@ -631,8 +631,8 @@ struct FastShared {
 // test 16 e^2 <= 3 N |I - q| tol needs the noise of e and I - q, about
 // 2^-47 of the integral in double-single, well below 3 N tol / 16; at the
 // coarsest levels (N = 256) that noise reaches it for integrals near
-// 2^47 tol 48, so quadratures above 1/64 of that take FP64 tables.
-__device__ inline double ff_limit(double tol) { return 0x1p47 * tol * 0.75; }
+// 2^47 tol 48, so quadratures above 1/8 of that take FP64 tables.
+__device__ inline double ff_limit(double tol) { return 0x1p47 * tol * 6.0; }
 
 // --------------------------------------------------------------- type 1
 
@@ -1083,7 +1083,10 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
                                int k, int Nb, int nf, int c, int Lc, int la, int lb, const double *pzA,
                                const double *pcA, const double *pzB, const double *pcB, double dAC,
                                double dBC, int ncls, int pa0, int pb0, const double *map, const int *win,
-                               int &warn) {
+                               bool useFF, int &warn) {
+  // mixed path: useFF picks the double-single tables and sums for this pass
+  // (one copy of the common code for both precisions)
+  const bool inFF = kMixed && useFF;
   const int lane = threadIdx.x & 31, nA = 2 * J.maxLBS + 1;
   const int LE = J.maxLECP > 0 ? J.maxLECP : 1, LBE = J.maxLBS + LE, OL = J.largeOrder;
   const int TS = L.tab2Stride;
@@ -1182,7 +1185,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       // the pair's own exponents (no integer divide) unless a stale slot
       const double zaj = owner == k ? za : pzA[owner / Nb], zbj = owner == k ? zb : pzB[owner % Nb];
       double *e = tab + lane * TS;
-      if constexpr (kMixed) {
+      if (inFF) {
         // the same rows in double-single
         ff *U = (ff *)(e + 3), *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
         const ff rf = ff_from_double(r);
@@ -1235,7 +1238,7 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
       auto vis = [&](int t) { return c92_slot[t] <= end; };  // an upper slot
       double I = sI[q], p = sP[q], qv = sQ[q], res = 0;
       bool done = false;
-      if constexpr (kMixed) {
+      if (inFF) {
         auto val = [&](int t) {
           const ff *U = (const ff *)(entry(t) + 3), *R = U + LE, *Ka = R + nA, *Kb = Ka + LBE;
           return ff_mul(ff_mul(ff_mul(Ka[l1], Kb[l2]), U[l]), R[l3]);
@@ -1605,14 +1608,9 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       // mixed path: double-single tables only where their sums can take the
       // reference's decisions (ff_limit); larger integrals in FP64
       const bool ff2 = kMixed && __longlong_as_double((long long)S.estBits) < ff_limit(J.tol);
-      for (int k = warp; k < NP; k += kWarps) {
-        if (ff2)
-          t2_pair<kMixed>(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0,
-                          ph + Lm.ppMap, (const int *)(ph + Lm.ppWin), warn2);
-        else
-          t2_pair<false>(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0,
-                         ph + Lm.ppMap, (const int *)(ph + Lm.ppWin), warn2);
-      }
+      for (int k = warp; k < NP; k += kWarps)
+        t2_pair<kMixed>(J, Lm, W, S, k, Nb, nf, c, Lc, la, lb, pzA, pcA, pzB, pcB, dAC, dBC, ncls, pa0, pb0,
+                        ph + Lm.ppMap, (const int *)(ph + Lm.ppWin), ff2, warn2);
       __syncthreads();
       for (int q = tid; q < nf; q += NT) {
         double v = 0.0;
