@@ -728,6 +728,162 @@ static __device__ void rsh_column(const DevJob &J, int lmax, int m, double x, do
 // A group of G primitive pairs (p0 .. p0+G-1) of the type-1 block, by one
 // warp (src/type1.c:95-302); lane = (pair, quadrature).  Adds the group's terms
 // to the warp's per-combined-index accumulators H.
+// The mixed kernel's type-1 large-grid fallback of one primitive pair kk
+// (src/type1.c:149-196) for the lanes whose small-grid quadrature (l1, l2)
+// failed (`fail`), out of line so that the three pair-kind instances of the
+// group code share one copy of both precisions' tables and walks; est: the
+// lane's last small-grid estimate (the ff_limit guard).  Returns each failed
+// lane's result.
+static __device__ __noinline__ double t1_fallback_mixed(const DevJob &J, double *tab, int c, int Lc, int lab, int kk,
+                                                       double s, bool fail, double est, int l1, int l2, int Nb,
+                                                       const double *pzA, const double *pcA, const double *pzB,
+                                                       const double *pcB, double dAC, double dBC, int ws, int we,
+                                                       int pa0, int pb0, int &warn) {
+  constexpr bool kMixed = true;
+  const int lane = threadIdx.x & 31, lq = lab + 1, O = kSmallOrder, OL = J.largeOrder, TSf = 3 + 2 * lq;
+  const double *uL = J.uL + (size_t)c * O;
+  bool ffp;
+  {
+    const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(fail ? est : 0.0) >> 32);
+    const unsigned lim = (unsigned)((unsigned long long)__double_as_longlong(ff_limit(J.tol)) >> 32);
+    ffp = __reduce_max_sync(0xffffffffu, hi) < lim;
+  }
+  const double za = pzA[kk / Nb], ca = zeta_times(pcA[kk / Nb], za, pa0), zb = pzB[kk % Nb],
+               cb = zeta_times(pcB[kk % Nb], zb, pb0);
+  const double z = -za - zb, zd2 = -za * dAC * dAC - zb * dBC * dBC;
+  const double C2 = ca * cb;
+  const ff C2f = ff_from_double(C2), sf = ff_from_double(s);
+  double i1, i2;
+  fm06(za, zb, dAC, dBC, i1, i2);
+  const ff i1f = ff_from_double(i1);
+  // first point past both centres whose exponent is below the screen
+  // (src/type1.c:168-176).  Past both centres the exponent falls as r
+  // grows, so the predicate is monotone in the index: a 32-way search,
+  // first over the last points of 32 chunks, then inside the first chunk
+  // whose last point qualifies.
+  auto brk = [&](int n) {
+    const double r = i1 * J.xLarge[n] + i2, e = (z * r + s) * r + zd2;
+    return r > dAC && r > dBC && e < J.lnAcc1;
+  };
+  const int chunk = (OL + 31) / 32;
+  int nb = OL;
+  {
+    const int n = lane * chunk + chunk - 1 < OL ? lane * chunk + chunk - 1 : OL - 1;
+    const unsigned b = __ballot_sync(0xffffffffu, brk(n));
+    if (b) {
+      const int n0 = (__ffs(b) - 1) * chunk;
+      for (int c0 = n0; c0 < n0 + chunk && c0 < OL; c0 += 32) {
+        const int m = c0 + lane;
+        const unsigned b2 = __ballot_sync(0xffffffffu, m < n0 + chunk && m < OL && brk(m));
+        if (b2) {
+          nb = c0 + __ffs(b2) - 1;
+          break;
+        }
+      }
+    }
+  }
+  const int end = nb - 1;
+  double I2 = 0, p2 = 0, q2 = 0, res2 = 0;
+  bool done2 = !fail;
+  for (int s0 = 0; s0 < OL;) {
+    const int s1 = step_end92(s0) < OL ? step_end92(s0) : OL;
+    // the rows the quadratures still running read
+    const int kq = __reduce_max_sync(0xffffffffu, done2 ? 0 : l2);
+    const int rq = __reduce_max_sync(0xffffffffu, done2 ? 0 : l1);
+    for (int t = s0 + lane; t < s1; t += 32) {
+      int n = __ldg(J.s92 + t);
+      bool upper = t > 0 && ((t - 1) & 1);
+      // entry: K_l rows, then the rows w * C2 U_L e^(..) r^l
+      double *K = tab + (t - s0) * TSf, *WR = K + lq;
+      const double w = J.wLarge[n] * i1;
+      bool any = false;
+      if (n < nb && !(upper && n > end)) {
+        double r = i1 * J.xLarge[n] + i2, ex = (z * r + s) * r + zd2;
+        if (ex >= J.lnAcc1) {
+          if (ffp) {
+            ff *Kf = (ff *)K, *WRf = (ff *)WR;
+            const ff rf = ff_from_double(r);
+            ff v = ff_mul(ff_mul(J.wLf[n], i1f),
+                          ff_mul(C2f, ff_mul(channel_ff(J, c, Lc, rf), ff_exp(ff_from_double(ex)))));
+            any = v.hi != 0.0f;
+            bessel_ff(J, kq, ff_mul(sf, rf), Kf, 1);
+            WRf[0] = v;
+            for (int l = 1; l <= rq; l++) {
+              v = ff_mul(v, rf);
+              WRf[l] = v;
+            }
+          } else {
+            double v = w * (C2 * channel<kMixed>(J, c, Lc, r) * fast_exp(ex));
+            any = v != 0.0;
+            bessel_fast<kMixed>(J, kq, s * r, K, 1);
+            WR[0] = v;
+            for (int l = 1; l <= rq; l++) {
+              v *= r;
+              WR[l] = v;
+            }
+          }
+        }
+      } else if (__builtin_expect(n != nb && !upper && n < O && n >= ws && n < we, 0)) {
+        // beyond the break the reference integrates its small-grid buffers:
+        // exponent and U_L at index n, r^l and K_l at flat offset l*OL + n of
+        // rows written with the small grid's stride
+        double rs = J.xSmall[n], es = (z * rs + s) * rs;
+        if (es >= J.lnAcc1) {
+          const double v = w * (C2 * uL[n] * fast_exp(es));
+          any = v != 0.0;
+          for (int l = 0; l <= lab; l++) {
+            int f = l * OL + n, lr = f / O, nr = f % O;
+            bool ok = lr <= lab && nr >= ws && nr < we;
+            double xr = J.xSmall[nr], pw = 1.0;
+            for (int i = 0; i < lr && ok; i++) pw = xr * pw;
+            WR[l] = ok ? v * pw : 0.0;
+            K[l] = ok ? bessel_row(J, lr, s * xr) : 0.0;
+          }
+          if (ffp)  // the rows as ff, in place (entry l holds row l either way)
+            for (int l = 0; l <= lab; l++) {
+              ((ff *)WR)[l] = ff_from_double(WR[l]);
+              ((ff *)K)[l] = ff_from_double(K[l]);
+            }
+        }
+      }
+      if (!any) {  // zero bits read as 0.0 in FP64 and in ff alike
+        for (int l = 0; l <= kq; l++) K[l] = 0.0;
+        for (int l = 0; l <= rq; l++) WR[l] = 0.0;
+      }
+    }
+    __syncwarp();
+    if (!done2) {
+      auto vis = [&](int t) { return c92_slot[t] <= end; };
+      if (ffp) {
+        auto val = [&](int t) {
+          const ff *e = (const ff *)(tab + (t - s0) * TSf);
+          return ff_mul(e[lq + l1], e[l2]);
+        };
+        psm92_advance_ff(s0, s1, J.tol, val, vis, I2, p2, q2, done2, res2);
+      } else {
+        auto val = [&](int t) {
+          const double *e = tab + (t - s0) * TSf;
+          return e[lq + l1] * e[l2];
+        };
+        psm92_advance(s0, s1, J.tol, val, vis, I2, p2, q2, done2, res2);
+      }
+    }
+    __syncwarp();
+    s0 = s1;
+    if (__all_sync(0xffffffffu, done2)) break;
+  }
+  double out = 0.0;
+  if (fail) {
+    if (!done2) {
+      res2 = 16 * I2 / (3 * (c92_lvN[c92_nLevels - 1] + 1.0));
+      warn = 1;
+    }
+    out = res2;
+  }
+  __syncwarp();
+  return out;
+}
+
 template <bool kMixed, int kKind>
 static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *W, int c, int Lc,
                                     int la, int lb, const int *perm, int p0, int G, int Nb, const double *pzA,
@@ -909,13 +1065,15 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
     // mixed path: the pair's tables in double-single only where the sums of
     // its failed quadratures can take the reference's decisions (ff_limit,
     // judged on their last small-grid estimates); larger integrals in FP64
-    bool ffp = false;
     if constexpr (kMixed) {
       const double est = fail ? fabs(16 * q / (3 * c93_lvN[c93_nLevels - 1])) : 0.0;
-      const unsigned hi = (unsigned)((unsigned long long)__double_as_longlong(est) >> 32);
-      const unsigned lim = (unsigned)((unsigned long long)__double_as_longlong(ff_limit(J.tol)) >> 32);
-      ffp = __reduce_max_sync(0xffffffffu, hi) < lim;
+      const double r = t1_fallback_mixed(J, tab, c, Lc, lab, perm[p0 + gg], sc[gg * 6], fail, est, l1, l2, Nb, pzA,
+                                         pcA, pzB, pcB, dAC, dBC, ws, we, pa0, pb0, warn);
+      if (fail) Q[g * RQ + l1 * lq + l2] += r;
+      __syncwarp();
+      continue;
     }
+    constexpr bool ffp = false;
     const int kk = perm[p0 + gg];
     const double za = pzA[kk / Nb], ca = zeta_times(pcA[kk / Nb], za, pa0), zb = pzB[kk % Nb],
                  cb = zeta_times(pcB[kk % Nb], zb, pb0);
