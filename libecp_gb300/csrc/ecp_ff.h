@@ -172,7 +172,9 @@ constexpr float kInvL = 0x1.715476p+9f;
 // difference is exact by Sterbenz's lemma), exp(r) - 1 by its Taylor
 // polynomial to r^4 (truncation below 2^-50 for |r| <= ln2/1024), the
 // high-order part in plain FP32.  Results below 2^-126 are returned as 0;
-// the arguments here are <= 0 or small.  Relative error about 2^-46.
+// the arguments here are <= 0 or small.  Relative error about 2^-46 where the
+// result is above 2^-100 (x > -69); below that its low part leaves the float
+// range and the absolute error stays below 2^-140 (tests/test_ff.py).
 FF_HD ff ff_exp(ff x) {
   if (x.hi < -87.0f) return {0.0f, 0.0f};
   const float k = rintf(f_mul(x.hi, kInvL));
