@@ -88,3 +88,24 @@ def test_poisson_stream_latency(eg):
     assert r["requests"] == len(systems) and not r["errors"]
     lat = r["latency_ms"]
     assert 0 < lat["p50"] <= lat["p99"] <= lat["max"]
+
+
+def test_small_request_overtakes_a_large_one(eg):
+    """Continuous batching at unit granularity: a small request submitted
+    right after a large one finishes first (the large job's CTAs take a few
+    units each and the small job runs on a high-priority stream), and both
+    results equal the same calls made alone."""
+    big = W.batched_cluster(0)  # ~91k units, ~0.12 s of the whole GPU
+    rng = np.random.default_rng(5)
+    small = W.serving_molecule(rng, 6, 1)
+    ref_big = eg.get_integrals_info(big, mode=eg.ECPGB_FAST)[1]
+    ref_small = eg.get_integrals_info(small, mode=eg.ECPGB_FAST)[1]
+    with eg.Server(mode=eg.ECPGB_FAST, budget_bytes=8 << 30, slots=4) as sv:
+        sv.wait(sv.submit(big))  # warm: buffers, tables and schedules in place
+        ib = sv.submit(big)
+        isml = sv.submit(small)
+        rs = sv.wait(isml)
+        rb = sv.wait(ib)
+    assert np.array_equal(rs[1], np.triu(ref_small)) and np.array_equal(rb[1], np.triu(ref_big))
+    # the small request was done well inside the large one's run
+    assert rs[2]["msLatency"] < 0.5 * rb[2]["msLatency"], (rs[2], rb[2])
