@@ -616,7 +616,7 @@ struct FastShared {
   // primitive pairs ordered by kind (normal, band, zero)
   int ppBreak[kMaxContraction * kMaxContraction];
   int t1Count[3];
-  int failIdx[kWalkCap];
+  int failIdx[kWalkCap];        // the pass's failed items as (l, l1, l2, l3) bytes
   unsigned failMask[64];
   int nFail, nThis, nextBase;
   int t2Next;                   // next small-grid item to hand out
@@ -1385,10 +1385,8 @@ static __device__ void t2_pair(const DevJob &J, const FastSmem &L, double *W, co
     int n1 = 0, n2 = 0, n3 = 0;
     for (int q = lane, qi = 0; q < nf; q += 32, qi++) {
       if (doneBits[qi] & (1u << lane)) continue;
-      int v = S.failIdx[q], l = 0, qq = v;
-      while (qq >= J.itemCnt[ncls + l]) { qq -= J.itemCnt[ncls + l]; l++; }
-      int it = J.items[J.itemOff[ncls + l] + qq];
-      int l1 = it & 255, l2 = (it >> 8) & 255, l3 = it >> 16;
+      // the pass's item, decoded once when the pass was listed
+      const int v = S.failIdx[q], l = v & 255, l1 = (v >> 8) & 255, l2 = (v >> 16) & 255, l3 = v >> 24;
       auto entry = [&](int t) {  // a queued slot's table entry
         const unsigned word = needBits[t >> 5], bit = 1u << (t & 31);
         return tab + (pref[t >> 5] + __popc(word & (bit - 1u))) * TS;
@@ -1742,9 +1740,10 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
         int m1 = 0, m2 = 0, m3 = 0;
         for (; q < nItems && nf < kWalkCap; q++)
           if (S.failMask[q >> 5] & (1u << (q & 31))) {
-            S.failIdx[nf++] = q;
             int l, l1, l2, l3;
             item(q, l, l1, l2, l3);
+            // the item's (l, l1, l2, l3), one byte each (all below 16)
+            S.failIdx[nf++] = l | l1 << 8 | l2 << 16 | l3 << 24;
             mask |= 1u << l;
             m1 = l1 > m1 ? l1 : m1;
             m2 = l2 > m2 ? l2 : m2;
@@ -1773,9 +1772,8 @@ static __device__ void unit_fast(const DevJob &J, const long long u, FastShared 
       for (int q = tid; q < nf; q += NT) {
         double v = 0.0;
         for (int w = 0; w < kWarps; w++) v += ph[w * Lm.w2Stride + Lm.w2Part + q];
-        int l, l1, l2, l3;
-        item(S.failIdx[q], l, l1, l2, l3);
-        T[tidx(l, l1, l2, l3)] = v;
+        const int it = S.failIdx[q];
+        T[tidx(it & 255, (it >> 8) & 255, (it >> 16) & 255, it >> 24)] = v;
       }
       __syncthreads();
     }
