@@ -1021,8 +1021,9 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       }
       t = 3;
     }
+    // the current level's first and end slot, read once per level
+    int lvStart = k == 0 ? 3 : c93_lvEnd[k - 1], lvEnd = c93_lvEnd[k];
     while (t < s1) {
-      int lvStart = k == 0 ? 3 : c93_lvEnd[k - 1];
       if (t == lvStart) cnt = 0;
       int lo = c93_slot[t], hi = c93_slot[t + 1];
       double T = 0.0;
@@ -1035,7 +1036,7 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
       }
       if (!done) I += T;
       t += 2;
-      if (t == c93_lvEnd[k]) {
+      if (t == lvEnd) {
         int j = c93_lvJ[k], n = c93_lvN[k];
         if (!done) {
           p += (1 - j) * (I - q);
@@ -1050,6 +1051,8 @@ static __device__ void t1_group_run(const DevJob &J, const FastSmem &L, double *
           }
         }
         k++;
+        lvStart = lvEnd;
+        lvEnd = c93_lvEnd[k];  // k <= the level count, inside the 32-entry table
       }
     }
     __syncwarp();
